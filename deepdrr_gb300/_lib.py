@@ -1,0 +1,112 @@
+"""ctypes binding of ``libdrr_gb300.so`` (the C ABI declared in ``include/drr_gb300.h``).
+
+The shared library is built in-tree by ``deepdrr_gb300.build``. Loading fails loudly when it is
+missing: there is no CPU fallback for any entry point.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from pathlib import Path
+
+from . import build as _build
+
+DRR_OK = 0
+DRR_ERR_INVALID_ARGUMENT = 1
+DRR_ERR_UNSUPPORTED = 2
+DRR_ERR_CUDA = 3
+DRR_ERR_OUT_OF_MEMORY = 4
+
+DRR_DENSITY_F32 = 0
+DRR_DENSITY_F16 = 1
+DRR_DENSITY_BF16 = 2
+
+DRR_MAX_VOLUMES = 4
+DRR_MAX_MATERIALS = 16
+
+DRR_FLAG_ATTENUATE_OUTSIDE = 1 << 0
+DRR_FLAG_FULL_MARCH = 1 << 1
+
+# Every symbol the header declares; the CPU test suite checks that the library exports all of them.
+EXPORTED_SYMBOLS = (
+    "drr_volset_create", "drr_volset_destroy", "drr_tables_create", "drr_tables_destroy",
+    "drr_project", "drr_neglog", "drr_clip_upper", "drr_last_error", "drr_version",
+)
+
+
+class DrrError(RuntimeError):
+    """A non-OK status returned by libdrr_gb300."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__(f"[status {status}] {message}")
+        self.status = status
+
+
+class drr_volume_desc(ctypes.Structure):
+    _fields_ = [
+        ("density", ctypes.c_void_p),
+        ("labels", ctypes.c_void_p),
+        ("ni", ctypes.c_int32), ("nj", ctypes.c_int32), ("nk", ctypes.c_int32),
+        ("density_type", ctypes.c_int32),
+    ]
+
+
+class drr_project_args(ctypes.Structure):
+    _fields_ = [
+        ("width", ctypes.c_int32), ("height", ctypes.c_int32),
+        ("step", ctypes.c_float), ("max_ray_length", ctypes.c_float),
+        ("air_index", ctypes.c_int32), ("flags", ctypes.c_uint32),
+        ("n_views", ctypes.c_int32),
+        ("priority", ctypes.c_void_p), ("enabled", ctypes.c_void_p),
+        ("world_from_index", ctypes.c_void_p), ("source_world", ctypes.c_void_p),
+        ("ijk_from_world", ctypes.c_void_p),
+        ("intensity", ctypes.c_void_p), ("photon_prob", ctypes.c_void_p),
+        ("area_density", ctypes.c_void_p), ("solid_angle", ctypes.c_void_p),
+    ]
+
+
+_LIB = None
+
+
+def library_path() -> Path:
+    return _build.BUILD / _build.LIB_NAME
+
+
+def load(build_if_missing: bool = True) -> ctypes.CDLL:
+    """Load the library, building it first if it is absent and a toolkit is present."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = library_path()
+    if not path.exists() or os.environ.get("DEEPDRR_GB300_REBUILD") == "1":
+        if not build_if_missing:
+            raise RuntimeError(f"libdrr_gb300.so not found at {path}; run deepdrr_gb300.build.build()")
+        _build.build()
+    lib = ctypes.CDLL(str(path))
+    vp, i32, st = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int
+    lib.drr_volset_create.argtypes = [ctypes.POINTER(drr_volume_desc), i32, i32, vp, ctypes.POINTER(vp)]
+    lib.drr_volset_create.restype = st
+    lib.drr_volset_destroy.argtypes = [vp]
+    lib.drr_volset_destroy.restype = st
+    lib.drr_tables_create.argtypes = [vp, vp, vp, i32, i32, vp, ctypes.POINTER(vp)]
+    lib.drr_tables_create.restype = st
+    lib.drr_tables_destroy.argtypes = [vp]
+    lib.drr_tables_destroy.restype = st
+    lib.drr_project.argtypes = [vp, vp, ctypes.POINTER(drr_project_args), vp]
+    lib.drr_project.restype = st
+    lib.drr_neglog.argtypes = [vp, i32, ctypes.c_int64, ctypes.c_float, vp]
+    lib.drr_neglog.restype = st
+    lib.drr_clip_upper.argtypes = [vp, ctypes.c_int64, ctypes.c_float, vp]
+    lib.drr_clip_upper.restype = st
+    lib.drr_last_error.argtypes = []
+    lib.drr_last_error.restype = ctypes.c_char_p
+    lib.drr_version.argtypes = []
+    lib.drr_version.restype = ctypes.c_char_p
+    _LIB = lib
+    return lib
+
+
+def check(status: int) -> None:
+    if status != DRR_OK:
+        msg = load().drr_last_error().decode("utf-8", "replace")
+        raise DrrError(status, msg)

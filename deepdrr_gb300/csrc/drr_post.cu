@@ -1,0 +1,151 @@
+// drr_post.cu -- post-processing of rendered views on the GPU.
+//
+// drr_neglog restates deepdrr/utils/image_utils.py:18-58 (`_neglog`) for a stack of views:
+//   image += min(image) + epsilon      (per view; note it ADDS the minimum, as the reference does)
+//   image  = -log(image)
+//   image  = (image - min) / (max - min)  per view; if any view is constant, every view becomes 0
+// All arithmetic is float32 like the reference's numpy float32 arrays.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <string>
+
+#include "../../include/drr_gb300.h"
+
+namespace drr {
+void set_last_error(const std::string &msg);  // drr_api.cu
+}
+
+namespace {
+
+// Order-preserving map float -> uint32 so that atomicMin/atomicMax on the key order like floats.
+__device__ __forceinline__ unsigned int fkey(float f) {
+    unsigned int u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float kfloat(unsigned int k) {
+    unsigned int u = (k & 0x80000000u) ? (k & 0x7fffffffu) : ~k;
+    return __uint_as_float(u);
+}
+
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ unsigned int warp_min(unsigned int v) {
+    for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ unsigned int warp_max(unsigned int v) {
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// keys[view*3 + 0] = min(image), 1 = min(-log(.)), 2 = max(-log(.))
+__global__ void neglog_init(unsigned int *keys, int n_views) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n_views) {
+        keys[i * 3 + 0] = 0xffffffffu;
+        keys[i * 3 + 1] = 0xffffffffu;
+        keys[i * 3 + 2] = 0u;
+    }
+}
+
+__global__ void neglog_min(const float *__restrict__ img, int64_t npix, unsigned int *keys) {
+    const int view = blockIdx.y;
+    const float *x = img + (int64_t)view * npix;
+    unsigned int m = 0xffffffffu;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < npix; i += (int64_t)gridDim.x * blockDim.x)
+        m = min(m, fkey(x[i]));
+    m = warp_min(m);
+    if ((threadIdx.x & 31) == 0) atomicMin(&keys[view * 3 + 0], m);
+}
+
+__global__ void neglog_log(float *__restrict__ img, int64_t npix, float epsilon, unsigned int *keys) {
+    const int view = blockIdx.y;
+    float *x = img + (int64_t)view * npix;
+    const float shift = __fadd_rn(kfloat(keys[view * 3 + 0]), epsilon);
+    unsigned int lo = 0xffffffffu, hi = 0u;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < npix; i += (int64_t)gridDim.x * blockDim.x) {
+        float y = -logf(__fadd_rn(x[i], shift));
+        x[i] = y;
+        lo = min(lo, fkey(y));
+        hi = max(hi, fkey(y));
+    }
+    lo = warp_min(lo);
+    hi = warp_max(hi);
+    if ((threadIdx.x & 31) == 0) {
+        atomicMin(&keys[view * 3 + 1], lo);
+        atomicMax(&keys[view * 3 + 2], hi);
+    }
+}
+
+__global__ void neglog_scale(float *__restrict__ img, int64_t npix, int n_views, const unsigned int *keys) {
+    __shared__ int any_constant;
+    if (threadIdx.x == 0) {
+        int c = 0;
+        for (int v = 0; v < n_views; v++) c |= (keys[v * 3 + 1] == keys[v * 3 + 2]);
+        any_constant = c;
+    }
+    __syncthreads();
+    const int view = blockIdx.y;
+    float *x = img + (int64_t)view * npix;
+    const float lo = kfloat(keys[view * 3 + 1]);
+    const float range = __fsub_rn(kfloat(keys[view * 3 + 2]), lo);
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < npix; i += (int64_t)gridDim.x * blockDim.x)
+        x[i] = any_constant ? 0.0f : __fdiv_rn(__fsub_rn(x[i], lo), range);
+}
+
+__global__ void clip_upper(float *__restrict__ img, int64_t n, float upper) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        img[i] = fminf(img[i], upper);
+}
+
+int blocks_for(int64_t npix) {
+    int64_t b = (npix + kThreads * 4 - 1) / (kThreads * 4);
+    if (b > 1216) b = 1216;  // 152 SMs x 8
+    return b < 1 ? 1 : (int)b;
+}
+
+}  // namespace
+
+extern "C" drr_status drr_neglog(float *images, int32_t n_views, int64_t pixels_per_view, float epsilon,
+                                 void *stream) {
+    if (n_views == 0 || pixels_per_view == 0) return DRR_OK;
+    if (!images || n_views < 0 || pixels_per_view < 0 || n_views > 65535) {
+        drr::set_last_error("drr_neglog: bad arguments");
+        return DRR_ERR_INVALID_ARGUMENT;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    unsigned int *keys = nullptr;
+    cudaError_t e = cudaMallocAsync((void **)&keys, sizeof(unsigned int) * 3 * (size_t)n_views, s);
+    if (e != cudaSuccess) {
+        drr::set_last_error(std::string("drr_neglog: cudaMallocAsync: ") + cudaGetErrorString(e));
+        return DRR_ERR_OUT_OF_MEMORY;
+    }
+    dim3 grid(blocks_for(pixels_per_view), n_views);
+    neglog_init<<<(n_views + 255) / 256, 256, 0, s>>>(keys, n_views);
+    neglog_min<<<grid, kThreads, 0, s>>>(images, pixels_per_view, keys);
+    neglog_log<<<grid, kThreads, 0, s>>>(images, pixels_per_view, epsilon, keys);
+    neglog_scale<<<grid, kThreads, 0, s>>>(images, pixels_per_view, n_views, keys);
+    e = cudaGetLastError();
+    cudaFreeAsync(keys, s);
+    if (e != cudaSuccess) {
+        drr::set_last_error(std::string("drr_neglog: launch: ") + cudaGetErrorString(e));
+        return DRR_ERR_CUDA;
+    }
+    return DRR_OK;
+}
+
+extern "C" drr_status drr_clip_upper(float *images, int64_t n, float upper, void *stream) {
+    if (n == 0) return DRR_OK;
+    if (!images || n < 0) {
+        drr::set_last_error("drr_clip_upper: bad arguments");
+        return DRR_ERR_INVALID_ARGUMENT;
+    }
+    clip_upper<<<blocks_for(n), kThreads, 0, (cudaStream_t)stream>>>(images, n, upper);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        drr::set_last_error(std::string("drr_clip_upper: launch: ") + cudaGetErrorString(e));
+        return DRR_ERR_CUDA;
+    }
+    return DRR_OK;
+}

@@ -1,0 +1,375 @@
+"""``Projector``: the drop-in replacement of deepdrr.Projector for volume rendering.
+
+Mirrors deepdrr/projector/projector.py (deepdrr v1.2.2): the constructor signature and checks
+(projector.py:398-587), ``initialize`` / ``free`` / context manager (:1395-1771), ``project`` /
+``__call__`` (:655-707, :1773) with its return types (numpy float32 [H, W] for one view, [N, H, W]
+otherwise), and the post-processing order noise -> clip -> neglog (:691-702).
+
+Everything that touches the GPU goes through ``libdrr_gb300.so`` (hand-written sm_103a kernels
+behind a C ABI); PyTorch only provides device memory and the current CUDA stream. There is no
+CPU fallback: without a CUDA device ``initialize`` raises.
+
+Not carried over: meshes (OpenGL depth peeling), scatter (deprecated in the reference, raises),
+``mode`` (stored but unused by the reference as well).
+"""
+from __future__ import annotations
+
+import ctypes
+import logging
+import math
+import warnings
+from typing import List, Optional, Sequence, Union
+
+import numpy as np
+
+from . import _lib, geo
+from .tables import TableSource, build_tables
+from .volume import Volume
+
+log = logging.getLogger(__name__)
+
+
+class DeprecationError(Exception):
+    """Raised for deprecated features, like the reference (pyvista.DeprecationError)."""
+
+
+def _listify(x) -> list:
+    return list(x) if isinstance(x, (list, tuple)) else [x]
+
+
+class Projector:
+    def __init__(
+        self,
+        volume: Union[Volume, List[Volume]],
+        priorities: Optional[List[int]] = None,
+        camera_intrinsics: Optional[geo.CameraIntrinsicTransform] = None,
+        device=None,
+        step: float = 0.1,
+        mode: str = "linear",
+        spectrum: Union[np.ndarray, str] = "90KV_AL40",
+        add_scatter: Optional[bool] = None,
+        scatter_num: int = 0,
+        add_noise: bool = False,
+        photon_count: int = 10000,
+        threads: int = 8,
+        max_block_index: int = 65535,
+        collected_energy: bool = False,
+        neglog: bool = True,
+        intensity_upper_bound: Optional[float] = None,
+        attenuate_outside_volume: bool = False,
+        source_to_detector_distance: float = -1,
+        carm=None,
+        max_mesh_hits: int = 32,
+        mesh_layers: int = 2,
+        cuda_device_id: Optional[int] = None,
+        *,
+        density_dtype: str = "float32",
+        tables: Optional[TableSource] = None,
+    ) -> None:
+        self.cuda_device_id = cuda_device_id
+        self.mesh_layers = mesh_layers
+        vols = _listify(volume)
+        self.volumes: List[Volume] = []
+        for v in vols:
+            if isinstance(v, Volume):
+                self.volumes.append(v)
+            else:
+                raise ValueError(f"unrecognized Renderable type: {type(v)}.")
+        if priorities is None:
+            self.priorities = [len(self.volumes) - 1 - i for i in range(len(self.volumes))]
+        else:
+            self.priorities = []
+            for prio in priorities:
+                assert isinstance(prio, int), "missing priority, or priority is not an integer"
+                assert 0 <= prio < len(vols), "invalid priority outside range [0, NUM_VOLUMES)"
+                self.priorities.append(prio)
+        assert len(self.volumes) == len(self.priorities)
+
+        if carm is not None:
+            warnings.warn("carm is deprecated, use device instead", DeprecationWarning)
+            self.device = carm
+        else:
+            self.device = device
+        self._camera_intrinsics = camera_intrinsics
+        self.step = float(step)
+        self.mode = mode
+        self.spectrum = spectrum
+        self._source_to_detector_distance = source_to_detector_distance
+
+        if add_scatter is not None:
+            log.warning("add_scatter is deprecated. Set scatter_num instead.")
+            if scatter_num != 0:
+                raise ValueError("Only set scatter_num.")
+            self.scatter_num = 1e7 if add_scatter else 0
+        elif scatter_num < 0:
+            raise ValueError("scatter_num must be non-negative.")
+        else:
+            self.scatter_num = scatter_num
+        if self.scatter_num > 0 and self.device is None:
+            raise ValueError("Must provide device to simulate scatter.")
+        if self.scatter_num > 0:
+            raise DeprecationError("Scatter is deprecated.")
+
+        self.add_noise = add_noise
+        self.photon_count = photon_count
+        self.threads = threads
+        self.max_block_index = max_block_index
+        self.collected_energy = collected_energy
+        self.neglog = neglog
+        self.intensity_upper_bound = intensity_upper_bound
+        self.max_mesh_hits = max_mesh_hits
+        if self.max_mesh_hits < 4 or self.max_mesh_hits % 4 != 0:
+            raise ValueError("max_mesh_depth must be a multiple of 4 and >= 4")
+
+        all_mats = []
+        for v in self.volumes:
+            all_mats.extend(list(v.materials[0].keys()))
+        if attenuate_outside_volume:
+            all_mats.append("air")
+        self.all_materials = sorted(set(all_mats))
+        self.air_index = self.all_materials.index("air") if attenuate_outside_volume else 0
+        self.attenuate_outside_volume = attenuate_outside_volume
+
+        if density_dtype not in ("float32", "float16", "bfloat16"):
+            raise ValueError(f"density_dtype must be float32, float16 or bfloat16, got {density_dtype!r}")
+        self.density_dtype = density_dtype
+        self._tables_source = tables
+        if len(self.all_materials) > _lib.DRR_MAX_MATERIALS:
+            raise ValueError(f"at most {_lib.DRR_MAX_MATERIALS} materials are supported")
+        if tables is not None:
+            for mat in self.all_materials:
+                if not tables.has_material(mat):
+                    raise ValueError(f"Material {mat} not found in material database. Please check the material name.")
+        self.output_shape = None
+        self.initialized = False
+        self._volset = None
+        self._tables = None
+
+    # ---- properties of the reference -------------------------------------------------------
+    @property
+    def source_to_detector_distance(self) -> float:
+        if self.device is not None:
+            return self.device.source_to_detector_distance
+        return self._source_to_detector_distance
+
+    @property
+    def camera_intrinsics(self) -> geo.CameraIntrinsicTransform:
+        if self.device is not None:
+            return self.device.camera_intrinsics
+        if self._camera_intrinsics is not None:
+            return self._camera_intrinsics
+        raise RuntimeError("No device provided. Set the device attribute by passing `device=<device>` to the constructor.")
+
+    @camera_intrinsics.setter
+    def camera_intrinsics(self, value: geo.CameraIntrinsicTransform):
+        if self.device is not None:
+            raise RuntimeError("Cannot set camera intrinsics when a device is provided. Use the device's camera_intrinsics instead.")
+        if not isinstance(value, geo.CameraIntrinsicTransform):
+            raise TypeError(f"Expected geo.CameraIntrinsicTransform, got {type(value)} instead.")
+        self._camera_intrinsics = value
+
+    @property
+    def volume(self) -> Volume:
+        if len(self.volumes) != 1:
+            raise AttributeError("projector contains multiple volumes. Access them with `projector.volumes[i]`")
+        return self.volumes[0]
+
+    @property
+    def output_size(self) -> int:
+        return int(np.prod(self.output_shape))
+
+    # ---- lifecycle -------------------------------------------------------------------------
+    def initialize(self) -> None:
+        """Upload volumes (as textures) and spectrum tables to the GPU (projector.py:1395-1717)."""
+        if self.initialized:
+            raise RuntimeError("Close projector before initializing again.")
+        import torch
+
+        if not torch.cuda.is_available():
+            raise RuntimeError("deepdrr_gb300 needs a CUDA device; there is no CPU fallback")
+        lib = _lib.load()
+        dev_id = 0 if self.cuda_device_id is None else int(self.cuda_device_id)
+        self.torch_device = torch.device("cuda", dev_id)
+        stream = torch.cuda.current_stream(self.torch_device)
+        descs = (_lib.drr_volume_desc * len(self.volumes))()
+        keep = []
+        dtype_code = {"float32": _lib.DRR_DENSITY_F32, "float16": _lib.DRR_DENSITY_F16,
+                      "bfloat16": _lib.DRR_DENSITY_BF16}[self.density_dtype]
+        with torch.cuda.device(self.torch_device):
+            for i, v in enumerate(self.volumes):
+                # reference layout [i, j, k] -> texture layout [k][j][i] (projector.py:1469)
+                dens = torch.from_numpy(np.ascontiguousarray(v.data, dtype=np.float32)).to(self.torch_device)
+                dens = dens.permute(2, 1, 0).contiguous()
+                if self.density_dtype == "float16":
+                    dens = dens.half()
+                elif self.density_dtype == "bfloat16":
+                    dens = dens.bfloat16()
+                # label remap to the sorted material list (projector.py:1495-1519)
+                names, seg = v.materials
+                lut = np.zeros(max(names.values()) + 1 if names else 1, dtype=np.uint8)
+                for name, idx in names.items():
+                    if name in self.all_materials:
+                        lut[idx] = self.all_materials.index(name)
+                seg_t = torch.from_numpy(np.ascontiguousarray(seg.astype(np.int64))).to(self.torch_device)
+                lut_t = torch.from_numpy(lut).to(self.torch_device)
+                labels = lut_t[seg_t].permute(2, 1, 0).contiguous()
+                keep += [dens, labels]
+                d = descs[i]
+                d.density = dens.data_ptr()
+                d.labels = labels.data_ptr()
+                ni, nj, nk = v.shape
+                d.ni, d.nj, d.nk = ni, nj, nk
+                d.density_type = dtype_code
+            handle = ctypes.c_void_p()
+            _lib.check(lib.drr_volset_create(descs, len(self.volumes), len(self.all_materials),
+                                             ctypes.c_void_p(stream.cuda_stream), ctypes.byref(handle)))
+            self._volset = handle
+            energies, pdf, mu = build_tables(self.spectrum, self.all_materials, self._tables_source)
+            self._energies, self._pdf, self._mu = energies, pdf, mu
+            th = ctypes.c_void_p()
+            _lib.check(lib.drr_tables_create(energies.ctypes.data, pdf.ctypes.data, mu.ctypes.data,
+                                             energies.shape[0], mu.shape[1], ctypes.c_void_p(stream.cuda_stream),
+                                             ctypes.byref(th)))
+            self._tables = th
+        del keep
+        self.output_shape = tuple(self.camera_intrinsics.sensor_size) if (
+            self.device is not None or self._camera_intrinsics is not None) else None
+        self.initialized = True
+
+    def free(self) -> None:
+        """Release the device copies (projector.py:1719-1764)."""
+        if self.initialized:
+            lib = _lib.load()
+            if self._volset:
+                lib.drr_volset_destroy(self._volset)
+            if self._tables:
+                lib.drr_tables_destroy(self._tables)
+            self._volset = None
+            self._tables = None
+        self.initialized = False
+
+    def __enter__(self) -> "Projector":
+        self.initialize()
+        return self
+
+    def __exit__(self, type, value, tb) -> None:
+        self.free()
+
+    def __call__(self, *args, **kwargs):
+        return self.project(*args, **kwargs)
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    # ---- projection ------------------------------------------------------------------------
+    def _prepare_project(self, camera_projections):
+        if not self.initialized:
+            raise RuntimeError("Projector has not been initialized.")
+        if not camera_projections and self.device is None:
+            raise ValueError("must provide a camera projection object to the projector, unless imaging device "
+                             "(e.g. CArm) is provided")
+        if not camera_projections:
+            camera_projections = [self.device.get_camera_projection()]
+            self.max_ray_length = math.sqrt(self.device.source_to_detector_distance ** 2
+                                            + self.device.detector_height ** 2 + self.device.detector_width ** 2)
+        else:
+            self.max_ray_length = self.source_to_detector_distance * 4
+        return camera_projections
+
+    def project_tensors(self, *camera_projections, area_density: bool = False, solid_angle: bool = False,
+                        flags: int = 0, stream=None) -> dict:
+        """Render all views in one library call and keep the results on the GPU.
+
+        Returns torch tensors: ``intensity`` and ``photon_prob`` [N, H, W] (float32), and
+        optionally ``area_density`` [N, M, H, W] (g/cm^2) and ``solid_angle`` [N, H, W]."""
+        import torch
+
+        camera_projections = self._prepare_project(camera_projections)
+        views = [geo.view_arrays(p) for p in camera_projections]
+        W0, H0 = views[0][2], views[0][3]
+        if any((w, h) != (W0, H0) for _, _, w, h in views):
+            raise ValueError("all views of one call must share the sensor size")
+        n = len(views)
+        nv = len(self.volumes)
+        wfi = np.ascontiguousarray(np.stack([v[0] for v in views]), dtype=np.float64)
+        src = np.ascontiguousarray(np.stack([v[1] for v in views]), dtype=np.float64)
+        ijk = np.empty((n, nv, 3, 4), dtype=np.float64)
+        for i, vol in enumerate(self.volumes):
+            ijk[:, i] = np.asarray(vol.ijk_from_world.data[:3, :4])
+        prio = np.asarray(self.priorities, dtype=np.int32)
+        enabled = np.asarray([1 if v.enabled else 0 for v in self.volumes], dtype=np.int32)
+        dev = self.torch_device
+        M = len(self.all_materials)
+        out = {
+            "intensity": torch.empty((n, H0, W0), dtype=torch.float32, device=dev),
+            "photon_prob": torch.empty((n, H0, W0), dtype=torch.float32, device=dev),
+        }
+        if area_density:
+            out["area_density"] = torch.empty((n, M, H0, W0), dtype=torch.float32, device=dev)
+        if solid_angle or self.collected_energy:
+            out["solid_angle"] = torch.empty((n, H0, W0), dtype=torch.float32, device=dev)
+        a = _lib.drr_project_args()
+        a.width, a.height = W0, H0
+        a.step = self.step
+        a.max_ray_length = float(self.max_ray_length)
+        a.air_index = self.air_index
+        a.flags = flags | (_lib.DRR_FLAG_ATTENUATE_OUTSIDE if self.attenuate_outside_volume else 0)
+        a.n_views = n
+        a.priority = prio.ctypes.data
+        a.enabled = enabled.ctypes.data
+        a.world_from_index = wfi.ctypes.data
+        a.source_world = src.ctypes.data
+        a.ijk_from_world = ijk.ctypes.data
+        a.intensity = out["intensity"].data_ptr()
+        a.photon_prob = out["photon_prob"].data_ptr()
+        a.area_density = out["area_density"].data_ptr() if "area_density" in out else None
+        a.solid_angle = out["solid_angle"].data_ptr() if "solid_angle" in out else None
+        s = stream if stream is not None else torch.cuda.current_stream(dev)
+        _lib.check(_lib.load().drr_project(self._volset, self._tables, ctypes.byref(a),
+                                           ctypes.c_void_p(s.cuda_stream)))
+        self.output_shape = (W0, H0)
+        return out
+
+    def project(self, *camera_projections) -> np.ndarray:
+        """Render, post-process and return numpy float32 [H, W] (one view) or [N, H, W]."""
+        images = self.project_images(*camera_projections)
+        images = images.cpu().numpy()
+        return images[0] if images.shape[0] == 1 else images
+
+    def project_images(self, *camera_projections, stream=None):
+        """``project`` without the host copy: the post-processed [N, H, W] float32 images on the GPU."""
+        import torch
+
+        out = self.project_tensors(*camera_projections, stream=stream)
+        images = out["intensity"]
+        if self.collected_energy:
+            images = self._collected_energy(camera_projections, images, out["solid_angle"]).contiguous()
+        if self.add_noise:
+            raise NotImplementedError("Poisson noise is not implemented yet")
+        lib = _lib.load()
+        s = stream if stream is not None else torch.cuda.current_stream(self.torch_device)
+        sp = ctypes.c_void_p(s.cuda_stream)
+        n, h, w = images.shape
+        if self.intensity_upper_bound is not None:
+            _lib.check(lib.drr_clip_upper(images.data_ptr(), images.numel(), float(self.intensity_upper_bound), sp))
+        if self.neglog:
+            _lib.check(lib.drr_neglog(images.data_ptr(), n, h * w, 0.01, sp))
+        return images
+
+    def _collected_energy(self, camera_projections, intensity, solid_angle):
+        """projector.py:833-853: intensity * solid angle * photons / mean(solid angle) / pixel area."""
+        projs = self._prepare_project(camera_projections)
+        out = []
+        for i, proj in enumerate(projs):
+            fx = proj.intrinsic.fx
+            fy = proj.intrinsic.fy
+            px = self.source_to_detector_distance / fx
+            py = self.source_to_detector_distance / fy
+            sa = solid_angle[i]
+            e = intensity[i] * sa * self.photon_count / sa.mean()
+            out.append(e / (px * py))
+        import torch
+        return torch.stack(out)

@@ -1,0 +1,129 @@
+/*
+ * drr_gb300.h -- C ABI of the GB300-native DeepDRR volume projector (libdrr_gb300.so).
+ *
+ * The library renders digitally reconstructed radiographs of one or more CT volumes: a fixed-step
+ * ray march with trilinear density sampling and per-material label fractions, followed by
+ * polychromatic Beer-Lambert attenuation over an X-ray spectrum. All entry points are plain C:
+ * handles, host pointers for small per-view geometry, device pointers for volumes and images, and
+ * a CUDA stream. No torch types cross this boundary.
+ *
+ * Each entry point replaces a piece of the reference projector (deepdrr v1.2.2):
+ *   drr_volset_create   Projector.initialize texture setup, deepdrr/projector/projector.py:1464-1546
+ *                       and create_cuda_texture, projector.py:116-257
+ *   drr_tables_create   the spectrum / mass-attenuation upload of Projector.initialize,
+ *                       projector.py:1659-1686
+ *   drr_project         Projector._render_single + _update_object_locations + the projectKernel
+ *                       launch, projector.py:709-800, 802-831; kernel deepdrr/projector/project_kernel.cu:135-650
+ *   drr_*_destroy       Projector.free, projector.py:1719-1764
+ *
+ * Conventions. Volumes are stored i-fastest ([nk][nj][ni]), i.e. the reference's
+ * np.moveaxis(data, [0,1,2], [2,1,0]) layout (projector.py:1469). Images are row-major [H][W]
+ * (the reference kernel writes column-major and the host transposes, projector.py:786-792).
+ * Every call is stream-ordered on the stream it is given; a handle must not be used from two
+ * host threads at once without external synchronisation. Errors are returned as status codes and
+ * described by drr_last_error() (thread-local); no kernel traps.
+ */
+#ifndef DRR_GB300_H
+#define DRR_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    DRR_OK = 0,
+    DRR_ERR_INVALID_ARGUMENT = 1, /* the reference raises ValueError / AssertionError here */
+    DRR_ERR_UNSUPPORTED = 2,      /* a size or mode this build does not implement */
+    DRR_ERR_CUDA = 3,             /* a CUDA runtime call failed; see drr_last_error() */
+    DRR_ERR_OUT_OF_MEMORY = 4
+} drr_status;
+
+typedef enum {
+    DRR_DENSITY_F32 = 0, /* float32 densities, hardware-filtered like the reference */
+    DRR_DENSITY_F16 = 1, /* IEEE half densities, hardware-filtered, float32 accumulation */
+    DRR_DENSITY_BF16 = 2 /* bfloat16 densities, filtered in software, float32 accumulation */
+} drr_density_type;
+
+#define DRR_MAX_VOLUMES 4
+#define DRR_MAX_MATERIALS 16
+
+/* One CT volume. `density` and `labels` are DEVICE pointers owned by the caller; the library
+ * copies them into its own texture storage during drr_volset_create and does not keep them. */
+typedef struct {
+    const void *density;    /* [nk][nj][ni] of drr_density_type */
+    const uint8_t *labels;  /* [nk][nj][ni], material index into the projector's sorted material list */
+    int32_t ni, nj, nk;
+    int32_t density_type;   /* drr_density_type */
+} drr_volume_desc;
+
+typedef struct drr_volset drr_volset;
+typedef struct drr_tables drr_tables;
+
+/* Create the device-side copy of `n_volumes` volumes (textures) for an `n_materials` projector.
+ * Labels are checked on the device to be < n_materials. Synchronous with respect to `stream`.
+ * Replaces projector.py:1464-1546 (texture creation) and create_cuda_texture, projector.py:116-257. */
+drr_status drr_volset_create(const drr_volume_desc *volumes, int32_t n_volumes, int32_t n_materials,
+                             void *stream, drr_volset **out);
+drr_status drr_volset_destroy(drr_volset *set);
+
+/* Upload a spectrum and its mass-attenuation table. Host pointers:
+ *   energies_kev [n_bins], pdf [n_bins], mu_over_rho [n_bins][n_materials] (cm^2/g).
+ * Replaces projector.py:1659-1686. */
+drr_status drr_tables_create(const float *energies_kev, const float *pdf, const float *mu_over_rho,
+                             int32_t n_bins, int32_t n_materials, void *stream, drr_tables **out);
+drr_status drr_tables_destroy(drr_tables *tables);
+
+enum {
+    DRR_FLAG_ATTENUATE_OUTSIDE = 1 << 0, /* Projector(attenuate_outside_volume=True), project_kernel.cu:358-361,522-527,557-560 */
+    DRR_FLAG_FULL_MARCH = 1 << 1         /* march every step from minAlpha like the reference (no prefix skip); for testing */
+};
+
+/* Arguments of one drr_project call: `n_views` views of the same volume set. */
+typedef struct {
+    int32_t width, height;          /* detector size in pixels */
+    float step;                     /* ray step in world units (mm), Projector(step=...) */
+    float max_ray_length;           /* <= 0: unlimited; projector.py:641-650 */
+    int32_t air_index;              /* index of "air" in the sorted material list (attenuate flag) */
+    uint32_t flags;                 /* DRR_FLAG_* */
+    int32_t n_views;
+    const int32_t *priority;        /* host [n_volumes]; smaller number wins (projector.py:489-500) */
+    const int32_t *enabled;         /* host [n_volumes]; 0 = volume ignored */
+    const double *world_from_index; /* host [n_views][3][3]: ray(u,v) = W [u+0.5, v+0.5, 1] (camera
+                                       projection's world_from_index[:-1, :], projector.py:803) */
+    const double *source_world;     /* host [n_views][3]: source position in world (center_in_world) */
+    const double *ijk_from_world;   /* host [n_views][n_volumes][3][4]: each volume's IJK_from_world */
+    float *intensity;               /* device [n_views][H][W], keV per photon (required) */
+    float *photon_prob;             /* device [n_views][H][W] (required) */
+    float *area_density;            /* device [n_views][n_materials][H][W] in g/cm^2, or NULL */
+    float *solid_angle;             /* device [n_views][H][W] pixel solid angles (sr), or NULL;
+                                       project_kernel.cu:14-133 */
+} drr_project_args;
+
+/* Render `args->n_views` views into the caller's device buffers, asynchronously on `stream`.
+ * Replaces projector.py:709-800 and the projectKernel launch (project_kernel.cu:135-650). */
+drr_status drr_project(drr_volset *set, const drr_tables *tables, const drr_project_args *args, void *stream);
+
+/* In-place negative-log transform of `n_views` float32 images of `pixels_per_view` pixels each,
+ * on `stream`: per view x += min(x) + epsilon; x = -log(x); x = (x - min) / (max - min), and every
+ * view becomes 0 if any view is constant. Replaces deepdrr/utils/image_utils.py:18-58 (`_neglog`,
+ * applied by Projector.project at projector.py:700-702). Uses 12 bytes per view of stream-ordered
+ * scratch (cudaMallocAsync). */
+drr_status drr_neglog(float *images, int32_t n_views, int64_t pixels_per_view, float epsilon, void *stream);
+
+/* In-place min(x, upper) over `n` floats: Projector(intensity_upper_bound=...), projector.py:697-698. */
+drr_status drr_clip_upper(float *images, int64_t n, float upper, void *stream);
+
+/* Human-readable description of the last error raised on this host thread ("" if none). */
+const char *drr_last_error(void);
+
+/* Library version string. */
+const char *drr_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DRR_GB300_H */

@@ -1,0 +1,66 @@
+"""Shared helpers of the test suite: build the same scene for the product and for the oracle."""
+from __future__ import annotations
+
+from pathlib import Path
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+from deepdrr_gb300 import geo, tables
+from deepdrr_gb300.volume import Volume
+from oracle import oracle
+
+ROOT = Path(__file__).resolve().parent.parent
+GOLDEN_TABLES = ROOT / "tests" / "golden" / "tables.npz"
+
+
+def material_list(volumes: Sequence[Volume], attenuate: bool = False) -> List[str]:
+    mats = []
+    for v in volumes:
+        mats.extend(v.materials[0].keys())
+    if attenuate:
+        mats.append("air")
+    return sorted(set(mats))
+
+
+def labels_for(volume: Volume, all_materials: Sequence[str]) -> np.ndarray:
+    """Label remap of projector.py:1495-1519: volume material id -> index in the sorted list."""
+    names, seg = volume.materials
+    lut = np.zeros(max(names.values()) + 1, dtype=np.uint8)
+    for name, idx in names.items():
+        lut[idx] = all_materials.index(name)
+    return lut[seg]
+
+
+def oracle_scene(volumes: Sequence[Volume], proj, *, step: float = 0.1, spectrum="90KV_AL40",
+                 priorities: Optional[Sequence[int]] = None, attenuate: bool = False,
+                 max_ray_length: float = -4.0, frac_bits: int = 8, source=None) -> oracle.Scene:
+    src = source or tables.NpzTables(GOLDEN_TABLES)
+    mats = material_list(volumes, attenuate)
+    e, pdf, mu = tables.build_tables(spectrum, mats, src)
+    W, s, w, h = geo.view_arrays(proj)
+    vols = [dict(density=v.data, labels=labels_for(v, mats), ijk_from_world=v.ijk_from_world.data)
+            for v in volumes]
+    return oracle.Scene(vols, W, s, width=w, height=h, step=step, energies=e, pdf=pdf, mu=mu,
+                        priorities=priorities, enabled=[1 if v.enabled else 0 for v in volumes],
+                        max_ray_length=max_ray_length, attenuate_outside=attenuate,
+                        air_index=mats.index("air") if attenuate else 0, frac_bits=frac_bits)
+
+
+def uniform_cube(n: int = 32, density: float = 1.0, spacing: float = 1.0, material: str = "soft tissue") -> Volume:
+    data = np.full((n, n, n), density, dtype=np.float32)
+    origin = -(n - 1) / 2 * spacing * np.ones(3)
+    return Volume.from_parameters(data, {material: np.ones((n, n, n), dtype=bool)}, origin=origin,
+                                  spacing=(spacing,) * 3)
+
+
+def axis_view(direction, sensor=(16, 16), pixel=0.5, sdd=1000.0, fraction=0.5, point=(0.0, 0.0, 0.0),
+              up=(0.0, 0.0, 1.0)):
+    return geo.CameraProjection.from_view(point, direction, up, source_to_detector_distance=sdd, pixel_size=pixel,
+                                          sensor_size=sensor, source_to_point_fraction=fraction)
+
+
+def rel_err(a, b, floor: float = 0.0):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return np.abs(a - b) / np.maximum(np.abs(b), floor)

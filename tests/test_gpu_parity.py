@@ -1,0 +1,277 @@
+"""GPU parity tests: the CUDA projector against the oracle (CPU restatement), the reference's own
+projectKernel (compiled from the reference sources, driven by oracle/ref_harness.cu), and the
+texture unit itself.
+
+Tolerances (stated per test):
+  * product vs float32 oracle: 2e-6 relative on intensity / photon_prob, 2e-6 relative (+1e-7 g/cm^2)
+    on per-material area densities. The only differences allowed are expf (CUDA vs libm, <= 2 ulp)
+    and the texture unit's internal blend arithmetic;
+  * product vs reference kernel: 1e-4 relative on intensity, and per-material path lengths within
+    1e-5 relative (+1e-6 g/cm^2), the targets of the projector's specification.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():
+    pytest.skip("needs a CUDA GPU", allow_module_level=True)
+
+import deepdrr_gb300 as dd
+from deepdrr_gb300 import _lib, geo, tables
+from deepdrr_gb300.phantoms import (ct_phantom, implant_volume, random_rigid, random_views, simple_phantom_hu,
+                                    volume_from_hu)
+from oracle import oracle, ref_kernel
+
+from helpers import GOLDEN_TABLES, labels_for, material_list, oracle_scene, rel_err, uniform_cube
+
+pytestmark = pytest.mark.gpu
+
+
+class DeltaTables(tables.TableSource):
+    """One 1 keV bin with pdf 1 and mu/rho = 1 for material `name`, 0 otherwise: then
+    photon_prob = exp(-area_density[name]), which exposes the reference kernel's path lengths."""
+
+    SPECTRUM = np.array([[1000.0, 1.0]])
+
+    def __init__(self, name):
+        self.name = name
+
+    def spectrum(self, name):
+        return self.SPECTRUM
+
+    def has_material(self, material):
+        return True
+
+    def mu_over_rho(self, material, energies_kev, spectrum_name=None):
+        return np.full(np.shape(energies_kev), 1.0 if material == self.name else 0.0, dtype=np.float32)
+
+
+def run_product(volumes, projs, *, spectrum="90KV_AL40", source=None, priorities=None, attenuate=False,
+                flags=0, density_dtype="float32", solid_angle=False):
+    src = source or tables.NpzTables(GOLDEN_TABLES)
+    p = dd.Projector(volumes, priorities=priorities, spectrum=spectrum, step=0.1, tables=src, neglog=False,
+                     attenuate_outside_volume=attenuate, density_dtype=density_dtype)
+    with p:
+        out = p.project_tensors(*projs, area_density=True, solid_angle=solid_angle, flags=flags)
+        torch.cuda.synchronize()
+        return {k: v.cpu().numpy() for k, v in out.items()}
+
+
+def small_scene(seed=0, n=48, sensor=(24, 20), pixel=3.0, views=2):
+    vol = volume_from_hu(simple_phantom_hu(n, seed=seed))
+    projs = random_views(views, vol.center_in_world, seed=seed + 7, sphere_mm=5.0, cone_deg=30.0,
+                         sensor_size=sensor, pixel_size=pixel, fraction_range=(0.5, 0.7))
+    return [vol], projs
+
+
+# ---------------------------------------------------------------- the texture unit ------------
+
+def test_texture_linear_filter_matches_the_oracle_emulation():
+    """Pins the oracle's model of the texture unit: xB = x - 0.5, weights frac(xB) rounded to
+    8 fractional bits, clamp addressing (CUDA Programming Guide, texture fetching)."""
+    rng = np.random.default_rng(0)
+    vol_kji = rng.uniform(0.0, 2.0, size=(5, 6, 7)).astype(np.float32)
+    pts = [np.stack([1.0 + np.arange(4096) / 4096.0, np.full(4096, 2.5), np.full(4096, 1.5)], 1)]
+    pts.append(rng.uniform(-1.5, 8.5, size=(4096, 3)))
+    pts.append(np.stack([np.full(2048, 3.25), 0.5 + np.arange(2048) / 1024.0, rng.uniform(0, 5, 2048)], 1))
+    xyz = np.concatenate(pts).astype(np.float32)
+    hw = ref_kernel.probe_texture(0, vol_kji, xyz)
+    dens_ijk = vol_kji.transpose(2, 1, 0)
+    sc = oracle.Scene([dict(density=dens_ijk, labels=np.zeros(dens_ijk.shape, np.uint8), ijk_from_world=np.eye(4))],
+                      np.eye(3), np.zeros(3), width=1, height=1, step=0.1, energies=np.ones(1), pdf=np.ones(1),
+                      mu=np.ones((1, 1)), frac_bits=8)
+    emu = np.array([sc.tex_linear(0, *map(float, p)) for p in xyz], dtype=np.float64)
+    err = np.abs(hw - emu)
+    print(f"texture linear: max |hw - emulation| = {err.max():.3g} over {len(xyz)} fetches")
+    assert err.max() <= 4e-7, err.max()
+
+
+def test_texture_point_filter_is_floor():
+    rng = np.random.default_rng(1)
+    labs = rng.integers(0, 16, size=(4, 5, 6)).astype(np.uint8)
+    base = rng.integers(-1, 7, size=(3000, 3)).astype(np.float64)
+    eps = rng.choice([0.0, 1e-7, -1e-7, 1e-4, -1e-4, 0.5, 0.999, 0.9999999], size=(3000, 3))
+    xyz = (base + eps).astype(np.float32)
+    hw = ref_kernel.probe_texture(1, labs, xyz).astype(np.int64)
+    x = np.clip(np.floor(xyz[:, 0].astype(np.float64)), 0, 5).astype(int)
+    y = np.clip(np.floor(xyz[:, 1].astype(np.float64)), 0, 4).astype(int)
+    z = np.clip(np.floor(xyz[:, 2].astype(np.float64)), 0, 3).astype(int)
+    np.testing.assert_array_equal(hw, labs[z, y, x])
+
+
+# ---------------------------------------------------------------- product vs oracle -----------
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_forward_matches_float32_oracle(seed):
+    vols, projs = small_scene(seed)
+    got = run_product(vols, projs, spectrum="120KV_AL43")
+    for i, proj in enumerate(projs):
+        sc = oracle_scene(vols, proj, spectrum="120KV_AL43")
+        ref = sc.project("f32")
+        assert rel_err(got["intensity"][i], ref["intensity"]).max() <= 2e-6
+        assert rel_err(got["photon_prob"][i], ref["photon_prob"]).max() <= 2e-6
+        d = np.abs(got["area_density"][i] - ref["area_density"])
+        assert np.all(d <= 2e-6 * np.abs(ref["area_density"]) + 1e-7), d.max()
+
+
+def test_prefix_skip_equals_full_march_bitwise():
+    vols, projs = small_scene(3, views=3)
+    a = run_product(vols, projs)
+    b = run_product(vols, projs, flags=_lib.DRR_FLAG_FULL_MARCH)
+    for k in ("intensity", "photon_prob", "area_density"):
+        np.testing.assert_array_equal(a[k], b[k])
+
+
+def test_multi_volume_matches_oracle_and_full_march():
+    rng = np.random.default_rng(4)
+    a = volume_from_hu(simple_phantom_hu(40, seed=4))
+    b = volume_from_hu(simple_phantom_hu(24, seed=5), spacing=(1.3, 1.3, 1.3))
+    b.world_from_anatomical = random_rigid(rng, 8.0, 20.0)
+    c = implant_volume((16, 16, 12), seed=6)
+    c.world_from_anatomical = random_rigid(rng, 5.0, 30.0)
+    vols = [a, b, c]
+    projs = random_views(2, a.center_in_world, seed=8, sphere_mm=5.0, sensor_size=(20, 18), pixel_size=3.0)
+    got = run_product(vols, projs)
+    full = run_product(vols, projs, flags=_lib.DRR_FLAG_FULL_MARCH)
+    for k in ("intensity", "area_density"):
+        np.testing.assert_array_equal(got[k], full[k])
+    for i, proj in enumerate(projs):
+        ref = oracle_scene(vols, proj).project("f32")
+        assert rel_err(got["intensity"][i], ref["intensity"]).max() <= 2e-6
+        d = np.abs(got["area_density"][i] - ref["area_density"])
+        assert np.all(d <= 2e-6 * np.abs(ref["area_density"]) + 1e-7), d.max()
+
+
+def test_attenuate_outside_matches_oracle():
+    vols, projs = small_scene(6)
+    got = run_product(vols, projs, attenuate=True)
+    for i, proj in enumerate(projs):
+        ref = oracle_scene(vols, proj, attenuate=True).project("f32")
+        assert rel_err(got["intensity"][i], ref["intensity"]).max() <= 2e-6
+        d = np.abs(got["area_density"][i] - ref["area_density"])
+        assert np.all(d <= 2e-6 * np.abs(ref["area_density"]) + 1e-6), d.max()
+
+
+# ---------------------------------------------------------------- product vs reference kernel --
+
+def _need_ref(nv, m, att=False):
+    if not ref_kernel.available(nv, m, att):
+        pytest.skip("reference cubins not built (no reference sources where this tree was built)")
+
+
+@pytest.mark.parametrize("seed", [0, 2])
+def test_forward_matches_reference_kernel_intensity(seed):
+    vols, projs = small_scene(seed)
+    _need_ref(1, 3)
+    got = run_product(vols, projs, spectrum="90KV_AL40", solid_angle=True)
+    for i, proj in enumerate(projs):
+        sc = oracle_scene(vols, proj, spectrum="90KV_AL40")
+        ref = ref_kernel.project(sc, solid_angle=True)
+        assert rel_err(got["intensity"][i], ref["intensity"]).max() <= 1e-4
+        assert rel_err(got["photon_prob"][i], ref["photon_prob"]).max() <= 1e-4
+        assert rel_err(got["solid_angle"][i], ref["solid_angle"]).max() <= 1e-5
+
+
+def test_path_lengths_match_reference_kernel():
+    """Per-material path lengths within 1e-5 relative of the reference kernel's, read out through a
+    one-bin spectrum (photon_prob = exp(-AD_m))."""
+    vols, projs = small_scene(1)
+    mats = material_list(vols)
+    _need_ref(1, len(mats))
+    for m, name in enumerate(mats):
+        src = DeltaTables(name)
+        got = run_product(vols, projs, spectrum=DeltaTables.SPECTRUM, source=src)
+        for i, proj in enumerate(projs):
+            sc = oracle_scene(vols, proj, spectrum=DeltaTables.SPECTRUM, source=src)
+            ref = ref_kernel.project(sc)
+            ad_ref = -np.log(ref["photon_prob"].astype(np.float64))
+            ad_got = got["area_density"][i, m].astype(np.float64)
+            assert np.all(np.abs(ad_got - ad_ref) <= 1e-5 * ad_ref + 1e-6), (name, np.abs(ad_got - ad_ref).max())
+
+
+def test_multi_volume_matches_reference_kernel():
+    rng = np.random.default_rng(11)
+    a = volume_from_hu(simple_phantom_hu(40, seed=11))
+    b = implant_volume((16, 16, 12), seed=12)
+    b.world_from_anatomical = random_rigid(rng, 5.0, 30.0)
+    vols = [a, b]
+    mats = material_list(vols)
+    _need_ref(2, len(mats))
+    projs = random_views(2, a.center_in_world, seed=13, sphere_mm=3.0, sensor_size=(20, 18), pixel_size=3.0)
+    got = run_product(vols, projs)
+    for i, proj in enumerate(projs):
+        ref = ref_kernel.project(oracle_scene(vols, proj))
+        assert rel_err(got["intensity"][i], ref["intensity"]).max() <= 1e-4
+
+
+def test_attenuate_outside_matches_reference_kernel():
+    vols, projs = small_scene(5)
+    mats = material_list(vols, attenuate=True)
+    assert mats[0] == "air"
+    _need_ref(1, len(mats), True)
+    got = run_product(vols, projs, attenuate=True)
+    for i, proj in enumerate(projs):
+        ref = ref_kernel.project(oracle_scene(vols, proj, attenuate=True))
+        assert rel_err(got["intensity"][i], ref["intensity"]).max() <= 1e-4
+
+
+# ---------------------------------------------------------------- post-processing and API ------
+
+def test_neglog_on_gpu_matches_the_restatement():
+    rng = np.random.default_rng(2)
+    img = rng.uniform(0.5, 60.0, size=(3, 33, 47)).astype(np.float32)
+    t = torch.from_numpy(img.copy()).cuda()
+    lib = _lib.load()
+    _lib.check(lib.drr_neglog(t.data_ptr(), 3, 33 * 47, 0.01, ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    torch.cuda.synchronize()
+    np.testing.assert_allclose(t.cpu().numpy(), oracle.neglog(img), atol=2e-6)
+    t = torch.ones((2, 8, 8), device="cuda")
+    _lib.check(lib.drr_neglog(t.data_ptr(), 2, 64, 0.01, None))
+    torch.cuda.synchronize()
+    assert float(t.abs().max()) == 0.0
+
+
+def test_projector_api_returns_reference_shapes():
+    vols, projs = small_scene(9, views=3)
+    src = tables.NpzTables(GOLDEN_TABLES)
+    with dd.Projector(vols, spectrum="90KV_AL40", tables=src, neglog=True, intensity_upper_bound=40.0) as p:
+        one = p.project(projs[0])
+        many = p(*projs)
+    assert one.shape == (20, 24) and one.dtype == np.float32
+    assert many.shape == (3, 20, 24)
+    assert 0.0 <= float(many.min()) and float(many.max()) <= 1.0
+    raw = run_product(vols, projs)["intensity"]
+    np.testing.assert_allclose(many, oracle.neglog(np.minimum(raw, 40.0)), atol=2e-6)
+
+
+def test_float16_density_error_against_float64_oracle():
+    """float16 density storage with float32 accumulation: the intensity error against the float64
+    oracle stays below 2e-3 relative (the float32 reference itself is ~5e-4 away from float64)."""
+    vols, projs = small_scene(4)
+    got = run_product(vols, projs, density_dtype="float16")
+    f32 = run_product(vols, projs)
+    for i, proj in enumerate(projs):
+        r64 = oracle_scene(vols, proj).project("f64")
+        e16 = rel_err(got["intensity"][i], r64["intensity"])
+        e32 = rel_err(f32["intensity"][i], r64["intensity"])
+        print(f"view {i}: fp16 max rel {e16.max():.3g} mean {e16.mean():.3g}; fp32 max rel {e32.max():.3g}")
+        assert e16.max() <= 2e-3
+
+
+def test_full_size_ct_view_matches_oracle_on_a_ray_subset():
+    """512 x 512 x 400 CT with titanium, one 1536^2 view: rays are independent, so the oracle on
+    2000 seeded pixels must reproduce the GPU image there."""
+    vols_projs = dd.phantoms.workload_ct(seed=0, views=1)
+    vols, projs = vols_projs[0], vols_projs[1]
+    got = run_product(vols, projs)
+    sc = oracle_scene(vols, projs[0])
+    rng = np.random.default_rng(5)
+    ids = rng.choice(1536 * 1536, size=2000, replace=False).astype(np.int64)
+    ref = sc.project("f32", ray_ids=ids)
+    gi = got["intensity"][0].ravel()[ids]
+    assert rel_err(gi, ref["intensity"]).max() <= 2e-6
+    gad = got["area_density"][0].reshape(4, -1)[:, ids]
+    d = np.abs(gad - ref["area_density"])
+    assert np.all(d <= 2e-6 * np.abs(ref["area_density"]) + 1e-7), d.max()
