@@ -40,9 +40,8 @@ drr_status cuda_fail(cudaError_t e, const char *what) {
 
 struct Volume {
     cudaArray_t density_array = nullptr;
-    cudaArray_t label_array = nullptr;
     cudaTextureObject_t density_tex = 0;
-    cudaTextureObject_t label_tex = 0;
+    uint32_t *packed = nullptr;   // [(nk+1)][(nj+1)][(ni+1)] 2x2x2 label words
     int ni = 0, nj = 0, nk = 0;
     int density_type = DRR_DENSITY_F32;
 };
@@ -96,13 +95,43 @@ drr_status make_texture(const void *src, int elem_bytes, cudaChannelFormatDesc f
 
 void free_volume(Volume &v) {
     if (v.density_tex) cudaDestroyTextureObject(v.density_tex);
-    if (v.label_tex) cudaDestroyTextureObject(v.label_tex);
     if (v.density_array) cudaFreeArray(v.density_array);
-    if (v.label_array) cudaFreeArray(v.label_array);
+    if (v.packed) cudaFree(v.packed);
     v = Volume();
 }
 
+// Label words of every base of a volume (see drr::pack_labels_kernel), owned by the volume set.
+drr_status make_label_tables(const uint8_t *src, int ni, int nj, int nk, cudaStream_t s, Volume &v) {
+    const size_t np = (size_t)(ni + 1) * (nj + 1) * (nk + 1);
+    DRR_CUDA_TRY(cudaMalloc(&v.packed, np * sizeof(uint32_t)), "cudaMalloc (packed labels)");
+    const size_t blocks = (np + 255) / 256;
+    drr::pack_labels_kernel<<<(unsigned)(blocks < 1048576 ? blocks : 1048576), 256, 0, s>>>(src, ni, nj, nk,
+                                                                                           v.packed);
+    DRR_CUDA_TRY(cudaGetLastError(), "pack_labels_kernel launch");
+    return DRR_OK;
+}
+
 }  // namespace
+
+namespace drr {
+__global__ void pack_labels_kernel(const uint8_t *__restrict__ labels, int ni, int nj, int nk, uint32_t *packed) {
+    const size_t np = (size_t)(ni + 1) * (nj + 1) * (nk + 1);
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < np; e += (size_t)gridDim.x * blockDim.x) {
+        const int bi = (int)(e % (ni + 1)) - 1;
+        const int bj = (int)((e / (ni + 1)) % (nj + 1)) - 1;
+        const int bk = (int)(e / ((size_t)(ni + 1) * (nj + 1))) - 1;
+        uint32_t word = 0;
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+            const int i = clampi(bi + (c & 1), 0, ni - 1);
+            const int j = clampi(bj + ((c >> 1) & 1), 0, nj - 1);
+            const int k = clampi(bk + (c >> 2), 0, nk - 1);
+            word |= ((uint32_t)labels[((size_t)k * nj + j) * ni + i] & 15u) << (4 * c);
+        }
+        packed[e] = word;
+    }
+}
+}  // namespace drr
 
 namespace drr {
 void set_last_error(const std::string &msg) { g_last_error = msg; }
@@ -180,8 +209,7 @@ drr_status drr_volset_create(const drr_volume_desc *volumes, int32_t n_volumes, 
         st = make_texture(d.density, d.density_type == DRR_DENSITY_F16 ? 2 : 4, fd, true, d.ni, d.nj, d.nk, s,
                           &v.density_array, &v.density_tex);
         if (st != DRR_OK) break;
-        st = make_texture(d.labels, 1, cudaCreateChannelDesc(8, 0, 0, 0, cudaChannelFormatKindUnsigned), false, d.ni,
-                          d.nj, d.nk, s, &v.label_array, &v.label_tex);
+        st = make_label_tables(d.labels, d.ni, d.nj, d.nk, s, v);
     }
     unsigned int hmax[DRR_MAX_VOLUMES] = {0};
     if (st == DRR_OK) {
@@ -321,7 +349,13 @@ drr_status project_nv(drr_volset *set, const drr_tables *tab, const drr_project_
     for (int i = 0; i < NV; i++) {
         const Volume &v = set->vol[i];
         p.vol[i].density = v.density_tex;
-        p.vol[i].labels = v.label_tex;
+        p.vol[i].packed = v.packed;
+        p.vol[i].n[0] = v.ni;
+        p.vol[i].n[1] = v.nj;
+        p.vol[i].n[2] = v.nk;
+        p.vol[i].nm1[0] = (float)(v.ni - 1);
+        p.vol[i].nm1[1] = (float)(v.nj - 1);
+        p.vol[i].nm1[2] = (float)(v.nk - 1);
         p.vol[i].hi[0] = (float)(v.ni - 0.5);
         p.vol[i].hi[1] = (float)(v.nj - 0.5);
         p.vol[i].hi[2] = (float)(v.nk - 0.5);

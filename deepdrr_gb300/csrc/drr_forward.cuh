@@ -7,30 +7,41 @@
 //   * num_steps = ceil((maxAlpha - minAlpha) / step)    project_kernel.cu:334
 //   * float32 `alpha += step`, sample p = s + alpha r - 1 (the -1 voxel offset of both fields)
 //                                                       project_kernel.cu:398-404, 552
-//   * label fetches on voxel change, one cache shared by all volumes   project_kernel.cu:394-431
+//   * labels of the 2x2x2 neighbourhood re-read on voxel change, one cache shared by all volumes
+//                                                       project_kernel.cu:394-431
 //   * trilinear label fractions, priority resolution, trapezoid half weights, hardware-filtered
 //     density, per-material accumulation                project_kernel.cu:433-551
 //   * air tails, * step, / 10 (mm -> cm)                project_kernel.cu:358-361, 557-584
 //   * polychromatic Beer-Lambert                        project_kernel.cu:637-646
-// Every multiply-add is an explicit __fmaf_rn / __fmul_rn / __fadd_rn so the compiler cannot
-// re-associate or contract differently from the CPU oracle.
+// Every multiply-add is an explicit __fmaf_rn / __fmul_rn / __fadd_rn, grouped exactly as nvcc
+// contracts the reference's expressions (a*b + c*d + e -> fma(a, b, c*d) + e; a*b + c*d + e*f ->
+// fma(e, f, fma(a, b, c*d))), so sample positions are bit-identical to the reference kernel's.
 //
 // Differences from the reference, none of which changes a result:
 //   * per-volume state lives in registers (NV, M are template parameters) instead of the
 //     reference's 528-byte local-memory stack frame;
+//   * the eight labels of a 2x2x2 neighbourhood come from one 32-bit load of a precomputed
+//     packed table (4 bits per corner, clamp addressing folded in) instead of eight point-filtered
+//     texture fetches (fetch_label_word explains why this reads exactly the reference's texels);
 //   * steps before the first volume interval opens do no sampling (their float32 alpha sequence is
 //     still accumulated step by step, so every later sample position is bit-identical), and the
 //     march stops once alpha has passed the last interval. With more than one volume the last
 //     skipped step is replayed in full so the shared label cache enters the first live step in the
 //     reference's state. DRR_FLAG_FULL_MARCH disables both shortcuts;
-//   * a 2x2x2 label block whose eight labels agree takes a one-material path (adding +0.0f to the
-//     other materials, as the reference does, leaves them unchanged);
+//   * a neighbourhood whose eight labels agree adds to one material only (the reference adds
+//     w * 0 = +0.0f to the others, which leaves them unchanged); its running sum is kept in a
+//     register and written back when the material changes, which keeps the exact sequence of
+//     float32 additions of every material;
+//   * the reference's "all label weights zero" skip (project_kernel.cu:476-486) can never fire:
+//     the eight trilinear weights are non-negative and one of them is at least 1/8;
 //   * disabled volumes are ignored (the reference samples them with uninitialised directions);
-//     the label cache starts as label 0 (the reference leaves it uninitialised).
+//     the label cache starts empty where the reference leaves it uninitialised.
 #pragma once
 
 #include <cuda_runtime.h>
 #include <stdint.h>
+
+#include "drr_alpha.h"
 
 namespace drr {
 
@@ -43,11 +54,12 @@ constexpr int kMaxSteps = 1 << 26;      // longest march per ray; longer rays ar
 
 struct VolConst {
     cudaTextureObject_t density;  // linear filter, clamp, unnormalised coordinates
-    cudaTextureObject_t labels;   // point filter, clamp, unnormalised coordinates, uint8
+    const uint32_t *packed;       // [(nk+1)][(nj+1)][(ni+1)] label words, see pack_labels_kernel
+    int32_t n[3];                 // ni, nj, nk
     float hi[3];                  // n - 0.5 per axis (projector.py:1626-1634)
+    float nm1[3];                 // n - 1 per axis
     int32_t priority;
     int32_t enabled;
-    int32_t pad;
 };
 
 struct VolPose {
@@ -81,6 +93,14 @@ struct ForwardParams {
     ViewRec<NV> views[kViewsPerLaunch];
 };
 
+// ---- float32 groupings of the reference's dot products (see the file comment) ----------------
+__device__ __forceinline__ float ray_component(float u, float a, float v, float b, float c) {
+    return __fadd_rn(__fmaf_rn(u, a, __fmul_rn(v, b)), c);  // u*a + v*b + c
+}
+__device__ __forceinline__ float dot3(float a0, float x, float a1, float y, float a2, float z) {
+    return __fmaf_rn(a2, z, __fmaf_rn(a0, x, __fmul_rn(a1, y)));  // a0*x + a1*y + a2*z
+}
+
 // Pixel solid angle from two tetrahedra, project_kernel.cu:14-133 (Van Oosterom-Strackee formula).
 __device__ __forceinline__ float pixel_solid_angle(const float *w, int udx, int vdx) {
     float cx[4], cy[4], cz[4], cm[4];
@@ -90,23 +110,25 @@ __device__ __forceinline__ float pixel_solid_angle(const float *w, int udx, int 
     for (int c = 0; c < 4; c++) {
         float cu = (float)udx + cu_off[c];
         float cv = (float)vdx + cv_off[c];
-        cx[c] = __fmaf_rn(cu, w[0], __fmaf_rn(cv, w[1], w[2]));
-        cy[c] = __fmaf_rn(cu, w[3], __fmaf_rn(cv, w[4], w[5]));
-        cz[c] = __fmaf_rn(cu, w[6], __fmaf_rn(cv, w[7], w[8]));
-        cm[c] = sqrtf(cx[c] * cx[c] + cy[c] * cy[c] + cz[c] * cz[c]);
+        cx[c] = ray_component(cu, w[0], cv, w[1], w[2]);
+        cy[c] = ray_component(cu, w[3], cv, w[4], w[5]);
+        cz[c] = ray_component(cu, w[6], cv, w[7], w[8]);
+        cm[c] = __fsqrt_rn(dot3(cx[c], cx[c], cy[c], cy[c], cz[c], cz[c]));
     }
-    float kx = cy[0] * cz[2] - cz[0] * cy[2];
-    float ky = cz[0] * cx[2] - cx[0] * cz[2];
-    float kz = cx[0] * cy[2] - cy[0] * cx[2];
-    float d01 = cx[0] * cx[1] + cy[0] * cy[1] + cz[0] * cz[1];
-    float d02 = cx[0] * cx[2] + cy[0] * cy[2] + cz[0] * cz[2];
-    float d03 = cx[0] * cx[3] + cy[0] * cy[3] + cz[0] * cz[3];
-    float d12 = cx[1] * cx[2] + cy[1] * cy[2] + cz[1] * cz[2];
-    float d23 = cx[2] * cx[3] + cy[2] * cy[3] + cz[2] * cz[3];
-    float n012 = fabsf(cx[1] * kx + cy[1] * ky + cz[1] * kz);
-    float n023 = fabsf(cx[3] * kx + cy[3] * ky + cz[3] * kz);
-    float den012 = cm[0] * cm[1] * cm[2] + d01 * cm[2] + d02 * cm[1] + d12 * cm[0];
-    float den023 = cm[0] * cm[2] * cm[3] + d02 * cm[3] + d03 * cm[2] + d23 * cm[0];
+    const float kx = __fmaf_rn(cy[0], cz[2], -__fmul_rn(cz[0], cy[2]));
+    const float ky = __fmaf_rn(cz[0], cx[2], -__fmul_rn(cx[0], cz[2]));
+    const float kz = __fmaf_rn(cx[0], cy[2], -__fmul_rn(cy[0], cx[2]));
+    const float d01 = dot3(cx[0], cx[1], cy[0], cy[1], cz[0], cz[1]);
+    const float d02 = dot3(cx[0], cx[2], cy[0], cy[2], cz[0], cz[2]);
+    const float d03 = dot3(cx[0], cx[3], cy[0], cy[3], cz[0], cz[3]);
+    const float d12 = dot3(cx[1], cx[2], cy[1], cy[2], cz[1], cz[2]);
+    const float d23 = dot3(cx[2], cx[3], cy[2], cy[3], cz[2], cz[3]);
+    const float n012 = fabsf(dot3(cx[1], kx, cy[1], ky, cz[1], kz));
+    const float n023 = fabsf(dot3(cx[3], kx, cy[3], ky, cz[3], kz));
+    const float den012 = __fmaf_rn(d12, cm[0], __fmaf_rn(d02, cm[1],
+                         __fmaf_rn(__fmul_rn(cm[0], cm[1]), cm[2], __fmul_rn(d01, cm[2]))));
+    const float den023 = __fmaf_rn(d23, cm[0], __fmaf_rn(d03, cm[2],
+                         __fmaf_rn(__fmul_rn(cm[0], cm[2]), cm[3], __fmul_rn(d02, cm[3]))));
     float sa012 = 2.f * atan2f(n012, den012);
     if (sa012 < 0.0f) sa012 += 3.14159265358979f;
     float sa023 = 2.f * atan2f(n023, den023);
@@ -117,6 +139,89 @@ __device__ __forceinline__ float pixel_solid_angle(const float *w, int udx, int 
 __device__ __forceinline__ float add_air(float x) {
     // area_density[AIR_INDEX] += AIR_DENSITY: a float32 accumulator plus a double literal
     return (float)((double)x + kAirDensity);
+}
+
+__device__ __forceinline__ int clampi(int x, int lo, int hi) { return x < lo ? lo : (x > hi ? hi : x); }
+
+// The eight labels the reference fetches at p + (dx, dy, dz) (point filter: texel clamp(floor)),
+// corner c = dx | dy << 1 | dz << 2 at bits 4c, with (bx, by, bz) = floor(p).
+// The reference's +1 corners read texel floor(p (+) 1) in float32; that always equals floor(p) + 1
+// here because p = F (-) 1 with F = fma(alpha, r, s) a float: for |p| <= 2, p (+) 1 is exact
+// (Sterbenz), and above that 1 is a multiple of ulp(p) (up to |p| = 2^24, far outside any volume,
+// where both corners clamp to the same texel anyway). So one packed word per base suffices.
+__device__ __forceinline__ uint32_t fetch_label_word(const VolConst &V, float bx, float by, float bz) {
+    // packed entry of base clamp(b, -1, n-1) + 1 (bases outside behave like the clamped one)
+    const int i = (int)fminf(fmaxf(bx, -1.0f), V.nm1[0]) + 1;
+    const int j = (int)fminf(fmaxf(by, -1.0f), V.nm1[1]) + 1;
+    const int k = (int)fminf(fmaxf(bz, -1.0f), V.nm1[2]) + 1;
+    return __ldg(V.packed + ((size_t)k * (V.n[1] + 1) + j) * (V.n[0] + 1) + i);
+}
+
+__device__ __forceinline__ bool uniform_word(uint32_t w) { return w == (w & 15u) * 0x11111111u; }
+
+// Trilinear label weights (project_kernel.cu:441-448): corner c = dx | dy << 1 | dz << 2 has
+// weight xy[c & 3] * z[c >> 2], with xy the four products (1-fx|fx)(1-fy|fy) rounded first.
+// The reference adds each corner weight into seg[label] as seg = fma(xy, z, seg) (nvcc contracts
+// the product into the accumulation), which is what uniform_sum and label_fractions do.
+struct CornerWeights {
+    float xy[4];
+    float z[2];
+};
+__device__ __forceinline__ CornerWeights corner_weights(float fx, float fy, float fz) {
+    const float gx = __fsub_rn(1.0f, fx), gy = __fsub_rn(1.0f, fy), gz = __fsub_rn(1.0f, fz);
+    CornerWeights cw;
+    cw.xy[0] = __fmul_rn(gx, gy);
+    cw.xy[1] = __fmul_rn(fx, gy);
+    cw.xy[2] = __fmul_rn(gx, fy);
+    cw.xy[3] = __fmul_rn(fx, fy);
+    cw.z[0] = gz;
+    cw.z[1] = fz;
+    return cw;
+}
+
+// seg of a neighbourhood whose eight labels agree: all eight weights accumulated from 0.
+__device__ __forceinline__ float uniform_sum(const CornerWeights &cw) {
+    float s = __fmul_rn(cw.xy[0], cw.z[0]);  // fma(xy, z, 0.0f)
+#pragma unroll
+    for (int c = 1; c < 8; c++) s = __fmaf_rn(cw.xy[c & 3], cw.z[c >> 2], s);
+    return s;
+}
+
+// seg[m] = the corner weights labelled m, accumulated in corner order from 0.
+template <int M>
+__device__ __forceinline__ void label_fractions(uint32_t word, const CornerWeights &cw, float seg[M]) {
+#pragma unroll
+    for (int m = 0; m < M; m++) seg[m] = 0.0f;
+    if (uniform_word(word)) {
+        const float s = uniform_sum(cw);
+        const int L = (int)(word & 15u);
+#pragma unroll
+        for (int m = 0; m < M; m++)
+            if (m == L) seg[m] = s;
+    } else {
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+            const int L = (int)((word >> (4 * c)) & 15u);
+#pragma unroll
+            for (int m = 0; m < M; m++)
+                if (m == L) seg[m] = __fmaf_rn(cw.xy[c & 3], cw.z[c >> 2], seg[m]);
+        }
+    }
+}
+
+template <int M>
+__device__ __forceinline__ void store_ad(float ad[M], int m_sel, float val) {
+#pragma unroll
+    for (int m = 0; m < M; m++)
+        if (m == m_sel) ad[m] = val;
+}
+template <int M>
+__device__ __forceinline__ float load_ad(const float ad[M], int m_sel) {
+    float r = 0.0f;
+#pragma unroll
+    for (int m = 0; m < M; m++)
+        if (m == m_sel) r = ad[m];
+    return r;
 }
 
 template <int NV, int M>
@@ -134,10 +239,10 @@ __global__ void __launch_bounds__(kBlockThreads) forward_kernel(const __grid_con
     // ---- ray setup (project_kernel.cu:218-234) ----
     const float uf = (float)u + 0.5f;
     const float vf = (float)v + 0.5f;
-    float rx = __fmaf_rn(uf, view.w[0], __fmaf_rn(vf, view.w[1], view.w[2]));
-    float ry = __fmaf_rn(uf, view.w[3], __fmaf_rn(vf, view.w[4], view.w[5]));
-    float rz = __fmaf_rn(uf, view.w[6], __fmaf_rn(vf, view.w[7], view.w[8]));
-    const float ray_length = __fsqrt_rn(__fmaf_rn(rx, rx, __fmaf_rn(ry, ry, __fmul_rn(rz, rz))));
+    float rx = ray_component(uf, view.w[0], vf, view.w[1], view.w[2]);
+    float ry = ray_component(uf, view.w[3], vf, view.w[4], view.w[5]);
+    float rz = ray_component(uf, view.w[6], vf, view.w[7], view.w[8]);
+    const float ray_length = __fsqrt_rn(__fmaf_rn(rz, rz, __fmaf_rn(rx, rx, __fmul_rn(ry, ry))));
     const float inv_norm = __fdiv_rn(1.0f, ray_length);
     rx = __fmul_rn(rx, inv_norm);
     ry = __fmul_rn(ry, inv_norm);
@@ -155,9 +260,9 @@ __global__ void __launch_bounds__(kBlockThreads) forward_kernel(const __grid_con
         rxi[i] = ryi[i] = rzi[i] = 0.0f;
         if (!p.vol[i].enabled) continue;
         const float *A = view.vol[i].a;
-        rxi[i] = __fmaf_rn(A[0], rx, __fmaf_rn(A[1], ry, __fmul_rn(A[2], rz)));
-        ryi[i] = __fmaf_rn(A[3], rx, __fmaf_rn(A[4], ry, __fmul_rn(A[5], rz)));
-        rzi[i] = __fmaf_rn(A[6], rx, __fmaf_rn(A[7], ry, __fmul_rn(A[8], rz)));
+        rxi[i] = dot3(A[0], rx, A[1], ry, A[2], rz);
+        ryi[i] = dot3(A[3], rx, A[4], ry, A[5], rz);
+        rzi[i] = dot3(A[6], rx, A[7], ry, A[8], rz);
         const float r3[3] = {rxi[i], ryi[i], rzi[i]};
         float mn = 0.0f;
         float mx = p.max_ray_length > 0.0f ? p.max_ray_length : __int_as_float(0x7f800000);
@@ -217,158 +322,159 @@ __global__ void __launch_bounds__(kBlockThreads) forward_kernel(const __grid_con
     const int air = p.air_index;
     if (attenuate) {
         const double pre = (double)__fdiv_rn(minA, step) * kAirDensity;
-#pragma unroll
-        for (int m = 0; m < M; m++)
-            if (m == air) ad[m] = (float)((double)ad[m] + pre);
+        store_ad<M>(ad, air, (float)((double)load_ad<M>(ad, air) + pre));
     }
 
     float alpha = minA;
     int t = 0;
+    int t_end = num_steps;  // the march can stop here: no interval is open beyond it
     if (!p.full_march) {
-        // Skip the steps before any interval opens, keeping the float32 alpha sequence exact.
-        float prev_alpha = alpha;
-        while (t < num_steps && alpha < amin) {
-            prev_alpha = alpha;
-            alpha = __fadd_rn(alpha, step);
-            ++t;
-        }
-        if (NV > 1 && t > 0) {  // replay one skipped step to seed the shared label cache
-            alpha = prev_alpha;
-            --t;
+        // Skip the steps before any interval opens and stop after the last one closes; the float32
+        // alpha sequence is fast-forwarded exactly (drr_alpha.h), so later positions are unchanged.
+        if (amin <= amax) {
+            t = advance_alpha(&alpha, step, amin, num_steps, false);  // first alpha >= amin
+            if (NV > 1 && t > 0) {  // replay one skipped step to seed the shared label cache
+                alpha = minA;
+                t = advance_alpha(&alpha, step, __int_as_float(0x7f800000), t - 1, false);
+            }
+            float a_end = alpha;
+            t_end = t + advance_alpha(&a_end, step, amax, num_steps - t, true);  // first alpha > amax
+        } else {
+            t = t_end = num_steps;  // no volume is ever sampled
         }
         if (attenuate) {
-            for (int k = 0; k < t; k++) {
-#pragma unroll
-                for (int m = 0; m < M; m++)
-                    if (m == air) ad[m] = add_air(ad[m]);
-            }
+            float a = load_ad<M>(ad, air);
+            for (int k = 0; k < t; k++) a = add_air(a);
+            store_ad<M>(ad, air, a);
         }
     }
 
     // ---- the march (project_kernel.cu:398-553) ----
-    float pb0 = -1.0f, pb1 = -1.0f, pb2 = -1.0f;  // previous_coordinates
-    int vox[8];
-#pragma unroll
-    for (int c = 0; c < 8; c++) vox[c] = 0;
-    bool uni = true;  // all eight cached labels equal
-    int uni_label = 0;
+    float pb0 = __int_as_float(0x7fc00000), pb1 = pb0, pb2 = pb0;  // previous_coordinates (none yet)
+    uint32_t word = 0;
 
-    for (; t < num_steps; ++t) {
-        if (!p.full_march && alpha > amax) break;
-        float px[NV], py[NV], pz[NV];
-        float seg[NV][M];
-#pragma unroll
-        for (int vol = 0; vol < NV; vol++) {
-#pragma unroll
-            for (int m = 0; m < M; m++) seg[vol][m] = 0.0f;
-            px[vol] = py[vol] = pz[vol] = 0.0f;
-            if (!p.vol[vol].enabled) continue;
-            const float *s = view.vol[vol].s;
-            px[vol] = __fsub_rn(__fmaf_rn(alpha, rxi[vol], s[0]), 1.0f);
-            py[vol] = __fsub_rn(__fmaf_rn(alpha, ryi[vol], s[1]), 1.0f);
-            pz[vol] = __fsub_rn(__fmaf_rn(alpha, rzi[vol], s[2]), 1.0f);
-            const float bx = floorf(px[vol]), by = floorf(py[vol]), bz = floorf(pz[vol]);
+    if (NV == 1 && !p.full_march) {
+        // One volume between its entry and exit: n is 1 at every step and the label cache only
+        // ever holds this volume's labels. The trapezoid half weights (project_kernel.cu:537) apply
+        // to t = 0 and t = num_steps - 1 only, so those steps are peeled off the main loop.
+        const VolConst &V = p.vol[0];
+        const float sx = view.vol[0].s[0], sy = view.vol[0].s[1], sz = view.vol[0].s[2];
+        const float rx0 = rxi[0], ry0 = ryi[0], rz0 = rzi[0];
+        int cur_m = -1;      // material whose accumulator is held in cur_ad
+        float cur_ad = 0.0f;
+        int uni_label = -1;  // label of the cached neighbourhood if its eight labels agree, else -1
+        auto sample = [&](float wscale) {
+            const float px = __fsub_rn(__fmaf_rn(alpha, rx0, sx), 1.0f);
+            const float py = __fsub_rn(__fmaf_rn(alpha, ry0, sy), 1.0f);
+            const float pz = __fsub_rn(__fmaf_rn(alpha, rz0, sz), 1.0f);
+            const float bx = floorf(px), by = floorf(py), bz = floorf(pz);
+            const float fx = __fsub_rn(px, bx), fy = __fsub_rn(py, by), fz = __fsub_rn(pz, bz);
             if (bx != pb0 || by != pb1 || bz != pb2) {
-                const cudaTextureObject_t lt = p.vol[vol].labels;
-#pragma unroll
-                for (int dz = 0; dz <= 1; dz++)
-#pragma unroll
-                    for (int dy = 0; dy <= 1; dy++)
-#pragma unroll
-                        for (int dx = 0; dx <= 1; dx++)
-                            vox[dz * 4 + dy * 2 + dx] =
-                                (int)tex3D<unsigned char>(lt, __fadd_rn(px[vol], (float)dx),
-                                                          __fadd_rn(py[vol], (float)dy),
-                                                          __fadd_rn(pz[vol], (float)dz));
+                word = fetch_label_word(V, bx, by, bz);
+                uni_label = uniform_word(word) ? (int)(word & 15u) : -1;
                 pb0 = bx;
                 pb1 = by;
                 pb2 = bz;
-                uni_label = vox[0];
-                uni = true;
-#pragma unroll
-                for (int c = 1; c < 8; c++) uni = uni && (vox[c] == vox[0]);
             }
-            const float fx = __fsub_rn(px[vol], bx), fy = __fsub_rn(py[vol], by), fz = __fsub_rn(pz[vol], bz);
-            const float gx = __fsub_rn(1.0f, fx), gy = __fsub_rn(1.0f, fy), gz = __fsub_rn(1.0f, fz);
-            float w[8];
-            w[0] = __fmul_rn(__fmul_rn(gx, gy), gz);
-            w[1] = __fmul_rn(__fmul_rn(fx, gy), gz);
-            w[2] = __fmul_rn(__fmul_rn(gx, fy), gz);
-            w[3] = __fmul_rn(__fmul_rn(fx, fy), gz);
-            w[4] = __fmul_rn(__fmul_rn(gx, gy), fz);
-            w[5] = __fmul_rn(__fmul_rn(fx, gy), fz);
-            w[6] = __fmul_rn(__fmul_rn(gx, fy), fz);
-            w[7] = __fmul_rn(__fmul_rn(fx, fy), fz);
-            if (uni) {
-                float sum = w[0];
-#pragma unroll
-                for (int c = 1; c < 8; c++) sum = __fadd_rn(sum, w[c]);
-#pragma unroll
-                for (int m = 0; m < M; m++)
-                    if (m == uni_label) seg[vol][m] = sum;
-            } else {
-#pragma unroll
-                for (int m = 0; m < M; m++) {
-                    float acc = 0.0f;
-#pragma unroll
-                    for (int c = 0; c < 8; c++) acc = __fadd_rn(acc, vox[c] == m ? w[c] : 0.0f);
-                    seg[vol][m] = acc;
+            const CornerWeights cw = corner_weights(fx, fy, fz);
+            const float rho = tex3D<float>(V.density, __fadd_rn(px, 0.5f), __fadd_rn(py, 0.5f), __fadd_rn(pz, 0.5f));
+            const float wr = __fmul_rn(wscale, rho);
+            if (uni_label >= 0) {
+                const float s = uniform_sum(cw);
+                if (uni_label != cur_m) {
+                    if (cur_m >= 0) store_ad<M>(ad, cur_m, cur_ad);
+                    cur_ad = load_ad<M>(ad, uni_label);
+                    cur_m = uni_label;
                 }
+                cur_ad = __fmaf_rn(wr, s, cur_ad);
+            } else {
+                if (cur_m >= 0) store_ad<M>(ad, cur_m, cur_ad);
+                cur_m = -1;
+                float seg[M];
+                label_fractions<M>(word, cw, seg);
+#pragma unroll
+                for (int m = 0; m < M; m++) ad[m] = __fmaf_rn(wr, seg[m], ad[m]);
             }
+            alpha = __fadd_rn(alpha, step);
+        };
+        if (t < t_end && t == 0) {
+            sample(0.5f);
+            ++t;
         }
-
-        // priority resolution (project_kernel.cu:458-496)
-        int cur = NV, n = 0;
-#pragma unroll
-        for (int i = 0; i < NV; i++) {
-            if (!trace[i]) continue;
-            if (alpha < minv[i] || alpha > maxv[i]) continue;
-            bool allzero = true;
-#pragma unroll
-            for (int m = 0; m < M; m++) allzero = allzero && (seg[i][m] == 0.0f);
-            if (allzero) continue;
-            const int pr = p.vol[i].priority;
-            if (pr < cur) {
-                cur = pr;
-                n = 1;
-            } else if (pr == cur) {
-                n += 1;
-            }
+        const bool last_half = t < t_end && t_end == num_steps;
+        const int t_main = last_half ? t_end - 1 : t_end;
+        for (; t < t_main; ++t) sample(1.0f);
+        if (last_half) {
+            sample(0.5f);
+            ++t;
         }
-
-        if (n == 0) {
-            if (attenuate) {
-#pragma unroll
-                for (int m = 0; m < M; m++)
-                    if (m == air) ad[m] = add_air(ad[m]);
-            }
-        } else {
-            float weight = __fdiv_rn(1.0f, (float)n);
-            weight = __fmul_rn(weight, (0 == t || num_steps - 1 == t) ? 0.5f : 1.0f);
+        if (cur_m >= 0) store_ad<M>(ad, cur_m, cur_ad);
+    } else {
+        // Several volumes (or DRR_FLAG_FULL_MARCH): the reference's step, every volume every step.
+        for (; t < t_end; ++t) {
+            float px[NV], py[NV], pz[NV];
+            float seg[NV][M];
 #pragma unroll
             for (int vol = 0; vol < NV; vol++) {
-                // no range re-check, as in project_kernel.cu:541
-                if (trace[vol] && p.vol[vol].priority == cur) {
-                    const float rho = tex3D<float>(p.vol[vol].density, __fadd_rn(px[vol], 0.5f),
-                                                   __fadd_rn(py[vol], 0.5f), __fadd_rn(pz[vol], 0.5f));
-                    const float wr = __fmul_rn(weight, rho);
 #pragma unroll
-                    for (int m = 0; m < M; m++) ad[m] = __fmaf_rn(wr, seg[vol][m], ad[m]);
+                for (int m = 0; m < M; m++) seg[vol][m] = 0.0f;
+                px[vol] = py[vol] = pz[vol] = 0.0f;
+                if (!p.vol[vol].enabled) continue;
+                const float *s = view.vol[vol].s;
+                px[vol] = __fsub_rn(__fmaf_rn(alpha, rxi[vol], s[0]), 1.0f);
+                py[vol] = __fsub_rn(__fmaf_rn(alpha, ryi[vol], s[1]), 1.0f);
+                pz[vol] = __fsub_rn(__fmaf_rn(alpha, rzi[vol], s[2]), 1.0f);
+                const float bx = floorf(px[vol]), by = floorf(py[vol]), bz = floorf(pz[vol]);
+                const float fx = __fsub_rn(px[vol], bx), fy = __fsub_rn(py[vol], by), fz = __fsub_rn(pz[vol], bz);
+                if (bx != pb0 || by != pb1 || bz != pb2) {
+                    word = fetch_label_word(p.vol[vol], bx, by, bz);
+                    pb0 = bx;
+                    pb1 = by;
+                    pb2 = bz;
+                }
+                label_fractions<M>(word, corner_weights(fx, fy, fz), seg[vol]);
+            }
+
+            // priority resolution (project_kernel.cu:458-496)
+            int cur = NV, n = 0;
+#pragma unroll
+            for (int i = 0; i < NV; i++) {
+                if (!trace[i]) continue;
+                if (alpha < minv[i] || alpha > maxv[i]) continue;
+                const int pr = p.vol[i].priority;
+                if (pr < cur) {
+                    cur = pr;
+                    n = 1;
+                } else if (pr == cur) {
+                    n += 1;
                 }
             }
+
+            if (n == 0) {
+                if (attenuate) store_ad<M>(ad, air, add_air(load_ad<M>(ad, air)));
+            } else {
+                float weight = __fdiv_rn(1.0f, (float)n);
+                weight = __fmul_rn(weight, (0 == t || num_steps - 1 == t) ? 0.5f : 1.0f);
+#pragma unroll
+                for (int vol = 0; vol < NV; vol++) {
+                    // no range re-check, as in project_kernel.cu:541
+                    if (trace[vol] && p.vol[vol].priority == cur) {
+                        const float rho = tex3D<float>(p.vol[vol].density, __fadd_rn(px[vol], 0.5f),
+                                                       __fadd_rn(py[vol], 0.5f), __fadd_rn(pz[vol], 0.5f));
+                        const float wr = __fmul_rn(weight, rho);
+#pragma unroll
+                        for (int m = 0; m < M; m++) ad[m] = __fmaf_rn(wr, seg[vol][m], ad[m]);
+                    }
+                }
+            }
+            alpha = __fadd_rn(alpha, step);
         }
-        alpha = __fadd_rn(alpha, step);
     }
     if (attenuate) {
-        for (; t < num_steps; ++t) {
-#pragma unroll
-            for (int m = 0; m < M; m++)
-                if (m == air) ad[m] = add_air(ad[m]);
-        }
+        float a = load_ad<M>(ad, air);
+        for (; t < num_steps; ++t) a = add_air(a);
         const double post = (double)__fdiv_rn(__fsub_rn(ray_length, maxA), step) * kAirDensity;
-#pragma unroll
-        for (int m = 0; m < M; m++)
-            if (m == air) ad[m] = (float)((double)ad[m] + post);
+        store_ad<M>(ad, air, (float)((double)a + post));
     }
 #pragma unroll
     for (int m = 0; m < M; m++) ad[m] = __fdiv_rn(__fmul_rn(ad[m], step), 10.0f);
@@ -395,6 +501,10 @@ __global__ void __launch_bounds__(kBlockThreads) forward_kernel(const __grid_con
     }
     if (p.solid_angle != nullptr) p.solid_angle[vout * plane + pix] = pixel_solid_angle(view.w, u, v);
 }
+
+// Packs the labels of every 2x2x2 neighbourhood: word(b) for base b in [-1, n-1]^3 holds the labels
+// at clamp(b + d, 0, n - 1), corner c = dx | dy << 1 | dz << 2 in bits 4c..4c+3.
+__global__ void pack_labels_kernel(const uint8_t *__restrict__ labels, int ni, int nj, int nk, uint32_t *packed);
 
 // Host-side launcher, explicitly instantiated per (NV, M) in drr_inst_nv*.cu.
 template <int NV, int M>

@@ -79,7 +79,41 @@ typedef struct {
     int attenuate_outside;
     int air_index;
     int frac_bits;                 /* linear-filter weight precision in ORC_MODE_F32 (0 = exact) */
+    int fp_profile;                /* multiply-add grouping of ORC_MODE_F32, see dot3_* below */
 } orc_scene;
+
+/* Multiply-add groupings of the float32 dot products of the ray setup. The reference kernel's
+ * arithmetic is whatever grouping nvcc chose when it contracted a*b + c*d + e into FMAs; the
+ * grouping is selected by `fp_profile` (bits 0-1: pixel ray, 2-3: squared norm, 4-5: IJK
+ * direction, 6: sample position, 7: label-weight accumulation seg += xy * z as one fma) and
+ * pinned against the reference kernel by the GPU tests. */
+static inline float ray3(int mode, float u, float w0, float v, float w1, float w2) {
+    switch (mode) {
+        case 0: return fmaf(u, w0, fmaf(v, w1, w2));
+        case 1: return fmaf(u, w0, v * w1) + w2;
+        case 2: return fmaf(v, w1, u * w0) + w2;
+        default: return (u * w0 + v * w1) + w2;
+    }
+}
+static inline float norm2(int mode, float x, float y, float z) {
+    switch (mode) {
+        case 0: return fmaf(x, x, fmaf(y, y, z * z));
+        case 1: return fmaf(z, z, fmaf(x, x, y * y));
+        case 2: return fmaf(x, x, y * y) + z * z;
+        default: return fmaf(z, z, fmaf(y, y, x * x));
+    }
+}
+static inline float dot3(int mode, float a0, float x, float a1, float y, float a2, float z) {
+    switch (mode) {
+        case 0: return fmaf(a0, x, fmaf(a1, y, a2 * z));
+        case 1: return fmaf(a2, z, fmaf(a0, x, a1 * y));
+        case 2: return fmaf(a0, x, a1 * y) + a2 * z;
+        default: return fmaf(a2, z, fmaf(a1, y, a0 * x));
+    }
+}
+static inline float sample_pos(int mode, float alpha, float r, float s) {
+    return mode == 0 ? fmaf(alpha, r, s) - 1.0f : (s + alpha * r) - 1.0f;
+}
 
 static inline int clamp_index(double f, int n) {
     /* clamp addressing of an unnormalised texture coordinate already floored */
@@ -106,19 +140,61 @@ static inline double quantize_weight(double a, int frac_bits) {
     return floor(a * s + 0.5) / s;
 }
 
+/* Corner weights of the texture unit's 3D linear filter, in units of 1/256, from the per-axis
+ * fractions Ax, Ay, Az in [0, 256] (each frac(x - 0.5) rounded to the nearest 1/256). Measured on
+ * the GPU with one-hot 2x2x2 textures (tests/test_gpu_parity.py pins it): the z split is exact,
+ * the x split rounds the upper branch half-up, and the y split rounds half-up the upper branch of
+ * the dx = 1 columns and the lower branch of the dx = 0 columns. Corner c = dx | dy << 1 | dz << 2;
+ * the eight weights always sum to 256. */
+static void hw_corner_weights(int Ax, int Ay, int Az, int W[8]) {
+    for (int dz = 0; dz <= 1; dz++) {
+        int vz = dz ? Az : 256 - Az;
+        int hx = (vz * Ax + 128) >> 8;
+        for (int dx = 0; dx <= 1; dx++) {
+            int vx = dx ? hx : vz - hx;
+            int hy = dx ? (vx * Ay + 128) >> 8 : vx - ((vx * (256 - Ay) + 128) >> 8);
+            W[dx | 2 | (dz << 2)] = hy;
+            W[dx | (dz << 2)] = vx - hy;
+        }
+    }
+}
+
 /* cudaFilterModeLinear, clamp, unnormalised coordinates (CUDA Programming Guide, "Texture
- * Fetching", linear filtering): xB = x - 0.5, i = floor(xB), alpha = frac(xB) held with
- * `frac_bits` fractional bits, value = trilinear blend of texels i and i+1 on each axis. */
+ * Fetching", linear filtering): xB = x - 0.5, i = floor(xB), alpha = frac(xB), value = blend of
+ * texels i and i+1 on each axis. frac_bits = 8 models NVIDIA's texture unit: 8-bit per-axis
+ * fractions combined into 8-bit corner weights (hw_corner_weights), the blend summed exactly and
+ * rounded once to float32 by the caller. frac_bits = 0 blends with exact weights. */
 static double tex_linear(const orc_volume *v, double x, double y, double z, int frac_bits) {
     double xb = x - 0.5, yb = y - 0.5, zb = z - 0.5;
+    if (frac_bits == 8) {
+        /* the texture unit clamps the coordinate itself to [0, n-1] (texel-centre space) before
+         * splitting it into a texel index and a fraction; this matters through the staged
+         * rounding of the corner weights */
+        xb = xb < 0.0 ? 0.0 : (xb > v->ni - 1.0 ? v->ni - 1.0 : xb);
+        yb = yb < 0.0 ? 0.0 : (yb > v->nj - 1.0 ? v->nj - 1.0 : yb);
+        zb = zb < 0.0 ? 0.0 : (zb > v->nk - 1.0 ? v->nk - 1.0 : zb);
+    }
+    const float *T = v->density;
+    if (frac_bits == 8) {
+        /* fixed point with 8 fractional bits: fix = round(xB * 256), texel fix >> 8, weight fix & 255
+         * (a fraction that rounds up to 1 carries into the next texel with weight 0) */
+        const long fx = (long)floor(xb * 256.0 + 0.5), fy = (long)floor(yb * 256.0 + 0.5), fz = (long)floor(zb * 256.0 + 0.5);
+        const int ii[2] = {(int)(fx >> 8), clamp_index((double)((fx >> 8) + 1), v->ni)};
+        const int jj[2] = {(int)(fy >> 8), clamp_index((double)((fy >> 8) + 1), v->nj)};
+        const int kk[2] = {(int)(fz >> 8), clamp_index((double)((fz >> 8) + 1), v->nk)};
+        int W[8];
+        hw_corner_weights((int)(fx & 255), (int)(fy & 255), (int)(fz & 255), W);
+        double s = 0.0;
+        for (int c = 0; c < 8; c++) s += (double)W[c] * (double)T[vidx(v, ii[c & 1], jj[(c >> 1) & 1], kk[c >> 2])];
+        return s / 256.0;
+    }
     double fi = floor(xb), fj = floor(yb), fk = floor(zb);
-    double a = quantize_weight(xb - fi, frac_bits);
-    double b = quantize_weight(yb - fj, frac_bits);
-    double c = quantize_weight(zb - fk, frac_bits);
     int i0 = clamp_index(fi, v->ni), i1 = clamp_index(fi + 1.0, v->ni);
     int j0 = clamp_index(fj, v->nj), j1 = clamp_index(fj + 1.0, v->nj);
     int k0 = clamp_index(fk, v->nk), k1 = clamp_index(fk + 1.0, v->nk);
-    const float *T = v->density;
+    double a = quantize_weight(xb - fi, frac_bits);
+    double b = quantize_weight(yb - fj, frac_bits);
+    double c = quantize_weight(zb - fk, frac_bits);
     double c00 = (1 - a) * T[vidx(v, i0, j0, k0)] + a * T[vidx(v, i1, j0, k0)];
     double c10 = (1 - a) * T[vidx(v, i0, j1, k0)] + a * T[vidx(v, i1, j1, k0)];
     double c01 = (1 - a) * T[vidx(v, i0, j0, k1)] + a * T[vidx(v, i1, j0, k1)];
@@ -160,10 +236,13 @@ static double ray_f32(const orc_scene *sc, int u, int v, float *ad_out, float *I
     const float step = sc->step;
     float uf = (float)((double)u + 0.5);
     float vf = (float)((double)v + 0.5);
-    float rx = fmaf(uf, W[0], fmaf(vf, W[1], W[2]));
-    float ry = fmaf(uf, W[3], fmaf(vf, W[4], W[5]));
-    float rz = fmaf(uf, W[6], fmaf(vf, W[7], W[8]));
-    float ray_length = sqrtf(fmaf(rx, rx, fmaf(ry, ry, rz * rz)));
+    const int pr_ray = sc->fp_profile & 3, pr_norm = (sc->fp_profile >> 2) & 3;
+    const int pr_dir = (sc->fp_profile >> 4) & 3, pr_pos = (sc->fp_profile >> 6) & 1;
+    const int pr_seg = (sc->fp_profile >> 7) & 1;
+    float rx = ray3(pr_ray, uf, W[0], vf, W[1], W[2]);
+    float ry = ray3(pr_ray, uf, W[3], vf, W[4], W[5]);
+    float rz = ray3(pr_ray, uf, W[6], vf, W[7], W[8]);
+    float ray_length = sqrtf(norm2(pr_norm, rx, ry, rz));
     float inv = 1.0f / ray_length;
     rx *= inv;
     ry *= inv;
@@ -178,9 +257,9 @@ static double ray_f32(const orc_scene *sc, int u, int v, float *ad_out, float *I
         trace[i] = 0;
         if (!V->enabled) continue;
         const float *A = V->ijk_from_world;
-        rxi[i] = fmaf(A[0], rx, fmaf(A[1], ry, A[2] * rz));
-        ryi[i] = fmaf(A[4], rx, fmaf(A[5], ry, A[6] * rz));
-        rzi[i] = fmaf(A[8], rx, fmaf(A[9], ry, A[10] * rz));
+        rxi[i] = dot3(pr_dir, A[0], rx, A[1], ry, A[2], rz);
+        ryi[i] = dot3(pr_dir, A[4], rx, A[5], ry, A[6], rz);
+        rzi[i] = dot3(pr_dir, A[8], rx, A[9], ry, A[10], rz);
         const float r3[3] = {rxi[i], ryi[i], rzi[i]};
         const float hi[3] = {(float)(V->ni - 0.5), (float)(V->nj - 0.5), (float)(V->nk - 0.5)};
         const float lo = -0.5f;
@@ -231,9 +310,9 @@ static double ray_f32(const orc_scene *sc, int u, int v, float *ad_out, float *I
         for (int vol = 0; vol < NV; vol++) {
             const orc_volume *V = &sc->vol[vol];
             if (!V->enabled) continue;
-            px[vol] = fmaf(alpha, rxi[vol], V->source_ijk[0]) - 1.0f;
-            py[vol] = fmaf(alpha, ryi[vol], V->source_ijk[1]) - 1.0f;
-            pz[vol] = fmaf(alpha, rzi[vol], V->source_ijk[2]) - 1.0f;
+            px[vol] = sample_pos(pr_pos, alpha, rxi[vol], V->source_ijk[0]);
+            py[vol] = sample_pos(pr_pos, alpha, ryi[vol], V->source_ijk[1]);
+            pz[vol] = sample_pos(pr_pos, alpha, rzi[vol], V->source_ijk[2]);
             for (int m = 0; m < M; m++) seg[vol][m] = 0.0f;
             float bx = floorf(px[vol]), by = floorf(py[vol]), bz = floorf(pz[vol]);
             if (bx != prev[0] || by != prev[1] || bz != prev[2]) {
@@ -249,18 +328,16 @@ static double ray_f32(const orc_scene *sc, int u, int v, float *ad_out, float *I
             }
             float fx = px[vol] - bx, fy = py[vol] - by, fz = pz[vol] - bz;
             float gx = 1.0f - fx, gy = 1.0f - fy, gz = 1.0f - fz;
-            float w[8];
-            w[0] = gx * gy * gz;
-            w[1] = fx * gy * gz;
-            w[2] = gx * fy * gz;
-            w[3] = fx * fy * gz;
-            w[4] = gx * gy * fz;
-            w[5] = fx * gy * fz;
-            w[6] = gx * fy * fz;
-            w[7] = fx * fy * fz;
+            /* xy products, then one z factor per corner (project_kernel.cu:441-448) */
+            const float xy[4] = {gx * gy, fx * gy, gx * fy, fx * fy};
+            const float zf[2] = {gz, fz};
             for (int c = 0; c < 8; c++) {
                 int lab = vox[c];
-                if (lab >= 0 && lab < M) seg[vol][lab] += w[c];
+                if (lab < 0 || lab >= M) continue;
+                if (pr_seg) /* seg += xy * z contracted into one fma */
+                    seg[vol][lab] = fmaf(xy[c & 3], zf[c >> 2], seg[vol][lab]);
+                else
+                    seg[vol][lab] += xy[c & 3] * zf[c >> 2];
             }
         }
         int cur = NV, n = 0;

@@ -23,6 +23,14 @@ BUILD = HERE / "_build"
 LIB_PATH = BUILD / "libdrr_oracle.so"
 MAX_VOL = 8
 MAX_MAT = 16
+# Multiply-add grouping of the reference kernel as nvcc 13.0 compiles it for sm_103a (found by
+# matching the reference kernel's path lengths on GB300; see fp_profile in drr_oracle.c):
+#   pixel ray     fma(u, w0, v*w1) + w2            (1)
+#   squared norm  fma(z, z, fma(x, x, y*y))         (1 << 2)
+#   IJK direction fma(a2, z, fma(a0, x, a1*y))      (1 << 4)
+#   position      fma(alpha, r, s) - 1              (0 << 6)
+#   label weights seg = fma(xy, z, seg)             (1 << 7)
+REFERENCE_FP_PROFILE = 1 | (1 << 2) | (1 << 4) | (1 << 7)
 
 
 class _Volume(ctypes.Structure):
@@ -45,7 +53,7 @@ class _Scene(ctypes.Structure):
         ("n_bins", ctypes.c_int),
         ("energies", ctypes.c_void_p), ("pdf", ctypes.c_void_p), ("mu", ctypes.c_void_p),
         ("attenuate_outside", ctypes.c_int), ("air_index", ctypes.c_int),
-        ("frac_bits", ctypes.c_int),
+        ("frac_bits", ctypes.c_int), ("fp_profile", ctypes.c_int),
     ]
 
 
@@ -98,7 +106,7 @@ class Scene:
 
     def __init__(self, volumes, world_from_index, source_world, *, width, height, step, energies, pdf, mu,
                  priorities=None, enabled=None, max_ray_length=-1.0, attenuate_outside=False, air_index=0,
-                 frac_bits=8):
+                 frac_bits=8, fp_profile=None):
         nv = len(volumes)
         if nv > MAX_VOL:
             raise ValueError(f"the oracle holds at most {MAX_VOL} volumes")
@@ -154,6 +162,7 @@ class Scene:
         sc.attenuate_outside = int(bool(attenuate_outside))
         sc.air_index = int(air_index)
         sc.frac_bits = int(frac_bits)
+        sc.fp_profile = REFERENCE_FP_PROFILE if fp_profile is None else int(fp_profile)
         self.sc = sc
         self.n_materials = M
 

@@ -72,20 +72,44 @@ def test_texture_linear_filter_matches_the_oracle_emulation():
     """Pins the oracle's model of the texture unit: xB = x - 0.5, weights frac(xB) rounded to
     8 fractional bits, clamp addressing (CUDA Programming Guide, texture fetching)."""
     rng = np.random.default_rng(0)
-    vol_kji = rng.uniform(0.0, 2.0, size=(5, 6, 7)).astype(np.float32)
+    nk, nj, ni = 300, 140, 260
+    k, j, i = np.meshgrid(np.arange(nk), np.arange(nj), np.arange(ni), indexing="ij")
+    vol_kji = (((i * 73 + j * 151 + k * 37) % 1009) / 1009.0).astype(np.float32)
     pts = [np.stack([1.0 + np.arange(4096) / 4096.0, np.full(4096, 2.5), np.full(4096, 1.5)], 1)]
     pts.append(rng.uniform(-1.5, 8.5, size=(4096, 3)))
-    pts.append(np.stack([np.full(2048, 3.25), 0.5 + np.arange(2048) / 1024.0, rng.uniform(0, 5, 2048)], 1))
+    pts.append(np.stack([rng.uniform(-2, ni + 1, 8192), rng.uniform(-2, nj + 1, 8192), rng.uniform(-2, nk + 1, 8192)], 1))
     xyz = np.concatenate(pts).astype(np.float32)
     hw = ref_kernel.probe_texture(0, vol_kji, xyz)
     dens_ijk = vol_kji.transpose(2, 1, 0)
     sc = oracle.Scene([dict(density=dens_ijk, labels=np.zeros(dens_ijk.shape, np.uint8), ijk_from_world=np.eye(4))],
                       np.eye(3), np.zeros(3), width=1, height=1, step=0.1, energies=np.ones(1), pdf=np.ones(1),
                       mu=np.ones((1, 1)), frac_bits=8)
-    emu = np.array([sc.tex_linear(0, *map(float, p)) for p in xyz], dtype=np.float64)
-    err = np.abs(hw - emu)
-    print(f"texture linear: max |hw - emulation| = {err.max():.3g} over {len(xyz)} fetches")
-    assert err.max() <= 4e-7, err.max()
+    emu = np.array([np.float32(sc.tex_linear(0, *map(float, p))) for p in xyz])
+    rel = np.abs(hw.astype(np.float64) - emu) / np.abs(emu)
+    exact = np.mean(hw == emu)
+    print(f"texture linear: {exact:.4f} of {len(xyz)} fetches bit-identical, max rel {rel.max():.3g}")
+    assert exact >= 0.98 and rel.max() <= 2.5e-7  # within one float32 ulp
+
+
+def test_texture_corner_weights_follow_the_staged_rule():
+    """One-hot 2x2x2 textures expose the texture unit's eight corner weights: multiples of 1/256
+    from the rule in the oracle's hw_corner_weights (z split exact, x split rounds the upper branch
+    half up, y split rounds half up the upper branch of dx = 1 and the lower branch of dx = 0)."""
+    rng = np.random.default_rng(3)
+    abc = rng.uniform(0, 255.4 / 256, size=(4096, 3))  # fractions that do not carry into the next texel
+    abc[:1024] = np.floor(abc[:1024] * 512) / 512
+    xyz = (0.5 + abc).astype(np.float32)
+    A = np.floor((xyz.astype(np.float64) - 0.5) * 256 + 0.5).astype(int)
+    for corner in range(8):
+        vol = np.zeros((2, 2, 2), np.float32)
+        vol[corner >> 2, (corner >> 1) & 1, corner & 1] = 1.0
+        hw = ref_kernel.probe_texture(0, vol, xyz) * 256
+        dx, dy, dz = corner & 1, (corner >> 1) & 1, corner >> 2
+        vz = A[:, 2] if dz else 256 - A[:, 2]
+        hx = (vz * A[:, 0] + 128) >> 8
+        vx = hx if dx else vz - hx
+        hy = (vx * A[:, 1] + 128) >> 8 if dx else vx - ((vx * (256 - A[:, 1]) + 128) >> 8)
+        np.testing.assert_array_equal(hw, hy if dy else vx - hy)
 
 
 def test_texture_point_filter_is_floor():
@@ -186,9 +210,12 @@ def test_path_lengths_match_reference_kernel():
         for i, proj in enumerate(projs):
             sc = oracle_scene(vols, proj, spectrum=DeltaTables.SPECTRUM, source=src)
             ref = ref_kernel.project(sc)
-            ad_ref = -np.log(ref["photon_prob"].astype(np.float64))
+            pp = ref["photon_prob"].astype(np.float64)
+            ad_ref = -np.log(pp)
             ad_got = got["area_density"][i, m].astype(np.float64)
-            assert np.all(np.abs(ad_got - ad_ref) <= 1e-5 * ad_ref + 1e-6), (name, np.abs(ad_got - ad_ref).max())
+            # read-out noise: two float32 ulps of exp(-AD) (CUDA's expf is within 2 ulp)
+            noise = 2.0 * np.spacing(ref["photon_prob"]).astype(np.float64) / pp
+            assert np.all(np.abs(ad_got - ad_ref) <= 1e-5 * ad_ref + noise), (name, np.abs(ad_got - ad_ref).max())
 
 
 def test_multi_volume_matches_reference_kernel():
