@@ -45,7 +45,9 @@ def parse_args():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--views", type=int, default=32)
     ap.add_argument("--seed", type=int, default=0)
-    ap.add_argument("--density-dtype", default="float32", choices=["float32", "float16"])
+    ap.add_argument("--density-dtype", default="float32", choices=["float32", "float16", "bfloat16"])
+    ap.add_argument("--workload", default="ct", choices=["ct", "ct512"],
+                    help="ct: 512x512x400 CT, 90 kVp (default); ct512: 512^3 CT, 120 kVp")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--small", action="store_true", help="a 128^3 / 256^2 workload for quick checks")
@@ -111,6 +113,11 @@ def workload(args, rank: int):
     if args.small:
         vols, projs, kw = phantoms.workload_simple(seed=args.seed, views=args.views)
         name = f"simple128_det256_{args.views}views_120kV"
+    elif args.workload == "ct512":
+        vols, projs, kw = phantoms.workload_ct(seed=args.seed, views=args.views * (rank + 1), shape=(512, 512, 512),
+                                               spectrum="120KV_AL43")
+        projs = projs[args.views * rank:]
+        name = f"ct512x512x512_det1536_{args.views}views_120kV"
     else:
         vols, projs, kw = phantoms.workload_ct(seed=args.seed, views=args.views * (rank + 1))
         projs = projs[args.views * rank:]
@@ -279,7 +286,8 @@ def main():
     line = {
         "metric": METRIC, "value": value, "unit": "projections/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32" if args.density_dtype == "float32" else "f16-storage/f32",
+        "vs_baseline": None, "dtype": {"float32": "f32", "float16": "f16-storage/f32",
+                                       "bfloat16": "bf16-storage/f32"}[args.density_dtype],
         "data": "synthetic (seeded CT phantom with titanium; seeded C-arm poses)",
         "config": {"workload": name, "volume": list(vols[0].shape), "detector": [W, H], "views_per_step": nviews,
                    "materials": len(p.all_materials), "n_bins": int(p._energies.shape[0]), "step_mm": kw["step"],

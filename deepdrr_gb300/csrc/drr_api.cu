@@ -6,6 +6,7 @@
 //   Projector.initialize (tables)  projector.py:1659-1686 -> drr_tables_create()
 //   _update_object_locations       projector.py:802-831   -> pack_view()
 //   _render_single                 projector.py:709-800   -> drr_project()
+#include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
@@ -45,6 +46,18 @@ struct Volume {
     int ni = 0, nj = 0, nk = 0;
     int density_type = DRR_DENSITY_F32;
 };
+
+// bfloat16 -> float16, exact for 0 and |x| in [2^-14, 65504]; anything else raises *bad.
+__global__ void bf16_to_f16_kernel(const __nv_bfloat16 *__restrict__ in, size_t n, __half *out, unsigned int *bad) {
+    unsigned int local_bad = 0;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const float x = __bfloat162float(in[i]);
+        const float ax = fabsf(x);
+        if (!(ax == 0.0f || (ax >= 6.103515625e-05f && ax <= 65504.0f))) local_bad = 1;
+        out[i] = __float2half_rn(x);
+    }
+    if (local_bad) atomicOr(bad, 1u);
+}
 
 __global__ void max_label_kernel(const uint8_t *__restrict__ labels, size_t n, unsigned int *out) {
     unsigned int local = 0;
@@ -177,22 +190,24 @@ drr_status drr_volset_create(const drr_volume_desc *volumes, int32_t n_volumes, 
             return fail(DRR_ERR_INVALID_ARGUMENT, "drr_volset_create: volume " + std::to_string(i) + " has an empty extent");
         if (d.ni > 16384 || d.nj > 16384 || d.nk > 16384)
             return fail(DRR_ERR_UNSUPPORTED, "drr_volset_create: 3D textures are limited to 16384 texels per axis");
-        if (d.density_type != DRR_DENSITY_F32 && d.density_type != DRR_DENSITY_F16)
+        if (d.density_type != DRR_DENSITY_F32 && d.density_type != DRR_DENSITY_F16 &&
+            d.density_type != DRR_DENSITY_BF16)
             return fail(DRR_ERR_UNSUPPORTED, "drr_volset_create: volume " + std::to_string(i) +
-                                                 ": only float32 and float16 densities are implemented");
+                                                 ": unknown density type " + std::to_string(d.density_type));
     }
     cudaStream_t s = (cudaStream_t)stream;
     drr_volset *set = new (std::nothrow) drr_volset();
     if (!set) return fail(DRR_ERR_OUT_OF_MEMORY, "drr_volset_create: host allocation failed");
     set->n_volumes = n_volumes;
     set->n_materials = n_materials;
-    unsigned int *d_max = nullptr;
-    cudaError_t e = cudaMalloc(&d_max, sizeof(unsigned int) * DRR_MAX_VOLUMES);
+    unsigned int *d_max = nullptr;  // per-volume maximum label, then one range-violation flag
+    cudaError_t e = cudaMalloc(&d_max, sizeof(unsigned int) * (DRR_MAX_VOLUMES + 1));
     if (e != cudaSuccess) {
         delete set;
         return cuda_fail(e, "cudaMalloc (label check)");
     }
-    cudaMemsetAsync(d_max, 0, sizeof(unsigned int) * DRR_MAX_VOLUMES, s);
+    unsigned int *d_bad = d_max + DRR_MAX_VOLUMES;
+    cudaMemsetAsync(d_max, 0, sizeof(unsigned int) * (DRR_MAX_VOLUMES + 1), s);
     drr_status st = DRR_OK;
     for (int i = 0; i < n_volumes && st == DRR_OK; i++) {
         const drr_volume_desc &d = volumes[i];
@@ -203,11 +218,43 @@ drr_status drr_volset_create(const drr_volume_desc *volumes, int32_t n_volumes, 
         v.density_type = d.density_type;
         const size_t n = (size_t)d.ni * d.nj * d.nk;
         max_label_kernel<<<1216, 256, 0, s>>>(d.labels, n, d_max + i);
-        cudaChannelFormatDesc fd = d.density_type == DRR_DENSITY_F16
-                                       ? cudaCreateChannelDesc(16, 0, 0, 0, cudaChannelFormatKindFloat)
-                                       : cudaCreateChannelDesc(32, 0, 0, 0, cudaChannelFormatKindFloat);
-        st = make_texture(d.density, d.density_type == DRR_DENSITY_F16 ? 2 : 4, fd, true, d.ni, d.nj, d.nk, s,
-                          &v.density_array, &v.density_tex);
+        const bool half = d.density_type != DRR_DENSITY_F32;
+        const void *src = d.density;
+        __half *converted = nullptr;
+        if (d.density_type == DRR_DENSITY_BF16) {
+            // bfloat16 has no texture format; its values are exact in float16 between 2^-14 and
+            // 65504 (and 0), so the texture holds the same numbers in float16
+            e = cudaMalloc(&converted, n * sizeof(__half));
+            if (e != cudaSuccess) {
+                st = cuda_fail(e, "cudaMalloc (bfloat16 conversion)");
+                break;
+            }
+            cudaMemsetAsync(d_bad, 0, sizeof(unsigned int), s);
+            bf16_to_f16_kernel<<<1216, 256, 0, s>>>((const __nv_bfloat16 *)d.density, n, converted, d_bad);
+            unsigned int bad = 0;
+            e = cudaMemcpyAsync(&bad, d_bad, sizeof(bad), cudaMemcpyDeviceToHost, s);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+            if (e != cudaSuccess) {
+                cudaFree(converted);
+                st = cuda_fail(e, "bfloat16 conversion");
+                break;
+            }
+            if (bad) {
+                cudaFree(converted);
+                st = fail(DRR_ERR_UNSUPPORTED, "drr_volset_create: volume " + std::to_string(i) +
+                                                   " has bfloat16 densities outside float16's normal range "
+                                                   "(|x| in [2^-14, 65504] or 0); store it as float32");
+                break;
+            }
+            src = converted;
+        }
+        cudaChannelFormatDesc fd = half ? cudaCreateChannelDesc(16, 0, 0, 0, cudaChannelFormatKindFloat)
+                                        : cudaCreateChannelDesc(32, 0, 0, 0, cudaChannelFormatKindFloat);
+        st = make_texture(src, half ? 2 : 4, fd, true, d.ni, d.nj, d.nk, s, &v.density_array, &v.density_tex);
+        if (converted) {
+            cudaStreamSynchronize(s);
+            cudaFree(converted);
+        }
         if (st != DRR_OK) break;
         st = make_label_tables(d.labels, d.ni, d.nj, d.nk, s, v);
     }

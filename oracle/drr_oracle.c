@@ -61,7 +61,22 @@ typedef struct {
     /* float64 per-view geometry for ORC_MODE_F64 */
     double ijk_from_world_d[12];
     double source_ijk_d[3];
+    int half_filter;           /* density held in a float16 texture: the filtered sample is a float16 */
 } orc_volume;
+
+/* IEEE binary16 round-to-nearest-even of x (what a float16 texture returns after filtering). */
+static double round_to_half(double x) {
+    if (x == 0.0 || !isfinite(x)) return x;
+    double ax = fabs(x);
+    int e;
+    frexp(ax, &e); /* ax in [2^(e-1), 2^e) */
+    int ex = e - 1;
+    if (ex < -14) ex = -14; /* subnormal spacing 2^-24 */
+    double ulp = ldexp(1.0, ex - 10);
+    double r = nearbyint(ax / ulp) * ulp;
+    if (r > 65504.0) r = INFINITY;
+    return x < 0 ? -r : r;
+}
 
 typedef struct {
     int n_volumes;
@@ -369,8 +384,9 @@ static double ray_f32(const orc_scene *sc, int u, int v, float *ad_out, float *I
                 const orc_volume *V = &sc->vol[vol];
                 /* no range re-check here: project_kernel.cu:541 */
                 if (trace[vol] && V->priority == cur && V->enabled) {
-                    float rho = (float)tex_linear(V, (double)(px[vol] + 0.5f), (double)(py[vol] + 0.5f),
-                                                  (double)(pz[vol] + 0.5f), sc->frac_bits);
+                    double rho_d = tex_linear(V, (double)(px[vol] + 0.5f), (double)(py[vol] + 0.5f),
+                                              (double)(pz[vol] + 0.5f), sc->frac_bits);
+                    float rho = (float)(V->half_filter ? round_to_half(rho_d) : rho_d);
                     float wr = weight * rho;
                     for (int m = 0; m < M; m++) ad[m] = fmaf(wr, seg[vol][m], ad[m]);
                 }

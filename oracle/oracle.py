@@ -40,6 +40,7 @@ class _Volume(ctypes.Structure):
         ("priority", ctypes.c_int), ("enabled", ctypes.c_int),
         ("ijk_from_world", ctypes.c_float * 12), ("source_ijk", ctypes.c_float * 3),
         ("ijk_from_world_d", ctypes.c_double * 12), ("source_ijk_d", ctypes.c_double * 3),
+        ("half_filter", ctypes.c_int),
     ]
 
 
@@ -106,7 +107,7 @@ class Scene:
 
     def __init__(self, volumes, world_from_index, source_world, *, width, height, step, energies, pdf, mu,
                  priorities=None, enabled=None, max_ray_length=-1.0, attenuate_outside=False, air_index=0,
-                 frac_bits=8, fp_profile=None):
+                 frac_bits=8, fp_profile=None, half_filter=False):
         nv = len(volumes)
         if nv > MAX_VOL:
             raise ValueError(f"the oracle holds at most {MAX_VOL} volumes")
@@ -136,6 +137,7 @@ class Scene:
             cv.density = dens.ctypes.data
             cv.labels = labs.ctypes.data
             cv.priority = int(priorities[i])
+            cv.half_filter = int(bool(half_filter[i] if isinstance(half_filter, (list, tuple)) else half_filter))
             cv.enabled = int(bool(enabled[i]))
             a32 = A[:3, :4].astype(np.float32).ravel()
             for j in range(12):

@@ -34,17 +34,33 @@ def labels_for(volume: Volume, all_materials: Sequence[str]) -> np.ndarray:
 
 def oracle_scene(volumes: Sequence[Volume], proj, *, step: float = 0.1, spectrum="90KV_AL40",
                  priorities: Optional[Sequence[int]] = None, attenuate: bool = False,
-                 max_ray_length: float = -4.0, frac_bits: int = 8, source=None) -> oracle.Scene:
+                 max_ray_length: float = -4.0, frac_bits: int = 8, source=None,
+                 density_dtype: str = "float32") -> oracle.Scene:
+    """The oracle's scene for ``volumes`` seen from ``proj``. With a float16 / bfloat16
+    ``density_dtype`` the densities are rounded to that type and the filtered samples to float16,
+    which is what the projector's half-precision textures hold and return."""
     src = source or tables.NpzTables(GOLDEN_TABLES)
     mats = material_list(volumes, attenuate)
     e, pdf, mu = tables.build_tables(spectrum, mats, src)
     W, s, w, h = geo.view_arrays(proj)
-    vols = [dict(density=v.data, labels=labels_for(v, mats), ijk_from_world=v.ijk_from_world.data)
-            for v in volumes]
+    vols = [dict(density=quantize_density(v.data, density_dtype), labels=labels_for(v, mats),
+                 ijk_from_world=v.ijk_from_world.data) for v in volumes]
     return oracle.Scene(vols, W, s, width=w, height=h, step=step, energies=e, pdf=pdf, mu=mu,
                         priorities=priorities, enabled=[1 if v.enabled else 0 for v in volumes],
                         max_ray_length=max_ray_length, attenuate_outside=attenuate,
-                        air_index=mats.index("air") if attenuate else 0, frac_bits=frac_bits)
+                        air_index=mats.index("air") if attenuate else 0, frac_bits=frac_bits,
+                        half_filter=density_dtype != "float32")
+
+
+def quantize_density(data: np.ndarray, density_dtype: str) -> np.ndarray:
+    """Densities as stored: float32 unchanged, float16 / bfloat16 rounded to nearest even."""
+    if density_dtype == "float32":
+        return data
+    if density_dtype == "float16":
+        return data.astype(np.float16).astype(np.float32)
+    import torch
+
+    return torch.from_numpy(np.ascontiguousarray(data, dtype=np.float32)).bfloat16().float().numpy()
 
 
 def uniform_cube(n: int = 32, density: float = 1.0, spacing: float = 1.0, material: str = "soft tissue") -> Volume:

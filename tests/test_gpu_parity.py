@@ -273,18 +273,29 @@ def test_projector_api_returns_reference_shapes():
     np.testing.assert_allclose(many, oracle.neglog(np.minimum(raw, 40.0)), atol=2e-6)
 
 
-def test_float16_density_error_against_float64_oracle():
-    """float16 density storage with float32 accumulation: the intensity error against the float64
-    oracle stays below 2e-3 relative (the float32 reference itself is ~5e-4 away from float64)."""
+@pytest.mark.parametrize("dtype,bound", [("float16", 2e-3), ("bfloat16", 1e-2)])
+def test_half_precision_storage(dtype, bound):
+    """float16 / bfloat16 densities (a float16 texture; bfloat16 values are exact in it) with float32
+    accumulation: matches the oracle with rounded densities and float16 filtered samples, and stays
+    within `bound` (relative intensity) of the float64 oracle on the unrounded volume.
+
+    The texture unit's float16 blend is round-to-nearest of the exact blend for 99.7 % of fetches;
+    the rest (exact ties, and values just above a tie that its narrower internal sum puts below it)
+    land one float16 ulp away, so the model comparison allows 5e-5 relative."""
     vols, projs = small_scene(4)
-    got = run_product(vols, projs, density_dtype="float16")
+    got = run_product(vols, projs, density_dtype=dtype)
     f32 = run_product(vols, projs)
     for i, proj in enumerate(projs):
         r64 = oracle_scene(vols, proj).project("f64")
-        e16 = rel_err(got["intensity"][i], r64["intensity"])
+        e = rel_err(got["intensity"][i], r64["intensity"])
         e32 = rel_err(f32["intensity"][i], r64["intensity"])
-        print(f"view {i}: fp16 max rel {e16.max():.3g} mean {e16.mean():.3g}; fp32 max rel {e32.max():.3g}")
-        assert e16.max() <= 2e-3
+        print(f"{dtype} view {i}: vs float64 max rel {e.max():.3g} mean {e.mean():.3g} "
+              f"(float32 storage: max {e32.max():.3g} mean {e32.mean():.3g})")
+        assert e.max() <= bound
+        ref = oracle_scene(vols, proj, density_dtype=dtype).project("f32")
+        assert rel_err(got["intensity"][i], ref["intensity"]).max() <= 5e-5
+        d = np.abs(got["area_density"][i] - ref["area_density"])
+        assert np.all(d <= 5e-5 * np.abs(ref["area_density"]) + 2e-6), d.max()
 
 
 def test_full_size_ct_view_matches_oracle_on_a_ray_subset():
