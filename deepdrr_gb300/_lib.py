@@ -30,7 +30,7 @@ DRR_FLAG_FULL_MARCH = 1 << 1
 # Every symbol the header declares; the CPU test suite checks that the library exports all of them.
 EXPORTED_SYMBOLS = (
     "drr_volset_create", "drr_volset_destroy", "drr_tables_create", "drr_tables_destroy",
-    "drr_project", "drr_neglog", "drr_clip_upper", "drr_last_error", "drr_version",
+    "drr_project", "drr_neglog", "drr_neglog_noalloc", "drr_clip_upper", "drr_last_error", "drr_version",
 )
 
 
@@ -96,6 +96,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     lib.drr_project.restype = st
     lib.drr_neglog.argtypes = [vp, i32, ctypes.c_int64, ctypes.c_float, vp]
     lib.drr_neglog.restype = st
+    lib.drr_neglog_noalloc.argtypes = [vp, i32, ctypes.c_int64, ctypes.c_float, vp]
+    lib.drr_neglog_noalloc.restype = st
     lib.drr_clip_upper.argtypes = [vp, ctypes.c_int64, ctypes.c_float, vp]
     lib.drr_clip_upper.restype = st
     lib.drr_last_error.argtypes = []

@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <mutex>
 #include <string>
 
 #include "../../include/drr_gb300.h"
@@ -130,6 +131,84 @@ extern "C" drr_status drr_neglog(float *images, int32_t n_views, int64_t pixels_
     cudaFreeAsync(keys, s);
     if (e != cudaSuccess) {
         drr::set_last_error(std::string("drr_neglog: launch: ") + cudaGetErrorString(e));
+        return DRR_ERR_CUDA;
+    }
+    return DRR_OK;
+}
+
+// ---- drr_neglog_noalloc: the same transform with library-owned scratch -----------------------
+//
+// Some hosts cannot let a library allocate device memory: a renderer or simulator that owns the
+// allocator and pre-budgets every byte, a real-time loop where cudaMalloc/cudaFree would
+// synchronise the device, or a CUDA-graph-based pipeline that forbids allocation calls while it
+// records. For them this entry point keeps its 12 bytes per view of scratch in a fixed file-scope
+// device array instead of allocating it. Every GPU that loads the library holds the array
+// (kNoAllocMaxViews * 12 bytes = 48 KiB) until the process exits.
+namespace {
+
+constexpr int kNoAllocMaxViews = 4096;
+constexpr int kNoAllocMaxDevices = 64;
+
+static __device__ __align__(256) unsigned int g_neglog_scratch[3 * kNoAllocMaxViews];
+
+std::mutex g_scratch_mutex;
+unsigned int *g_scratch_address[kNoAllocMaxDevices] = {};
+
+// Device address of g_neglog_scratch on the current device. In host code the array's name is only
+// a host-side stand-in, so the address is looked up once per device (with that device current)
+// and cached.
+drr_status scratch_address(unsigned int **out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) {
+        drr::set_last_error(std::string("drr_neglog_noalloc: cudaGetDevice: ") + cudaGetErrorString(e));
+        return DRR_ERR_CUDA;
+    }
+    if (dev < 0 || dev >= kNoAllocMaxDevices) {
+        drr::set_last_error("drr_neglog_noalloc: device ordinal beyond the supported range");
+        return DRR_ERR_UNSUPPORTED;
+    }
+    std::lock_guard<std::mutex> lock(g_scratch_mutex);
+    if (g_scratch_address[dev] == nullptr) {
+        unsigned int *ptr = nullptr;
+        e = cudaGetSymbolAddress((void **)&ptr, g_neglog_scratch);
+        if (e != cudaSuccess || ptr == nullptr) {
+            drr::set_last_error(std::string("drr_neglog_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+            return DRR_ERR_CUDA;
+        }
+        g_scratch_address[dev] = ptr;
+    }
+    *out = g_scratch_address[dev];
+    return DRR_OK;
+}
+
+}  // namespace
+
+extern "C" drr_status drr_neglog_noalloc(float *images, int32_t n_views, int64_t pixels_per_view, float epsilon,
+                                         void *stream) {
+    if (n_views == 0 || pixels_per_view == 0) return DRR_OK;
+    if (!images || n_views < 0 || pixels_per_view < 0) {
+        drr::set_last_error("drr_neglog_noalloc: bad arguments");
+        return DRR_ERR_INVALID_ARGUMENT;
+    }
+    if (n_views > kNoAllocMaxViews) {
+        drr::set_last_error("drr_neglog_noalloc: " + std::to_string(n_views) + " views exceed the fixed scratch of " +
+                            std::to_string(kNoAllocMaxViews) + " views; split the call or use drr_neglog");
+        return DRR_ERR_UNSUPPORTED;
+    }
+    unsigned int *keys = nullptr;
+    drr_status st = scratch_address(&keys);
+    if (st != DRR_OK) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    dim3 grid(blocks_for(pixels_per_view), n_views);
+    // neglog_init resets the per-view minimum / maximum words the previous call left behind
+    neglog_init<<<(n_views + 255) / 256, 256, 0, s>>>(keys, n_views);
+    neglog_min<<<grid, kThreads, 0, s>>>(images, pixels_per_view, keys);
+    neglog_log<<<grid, kThreads, 0, s>>>(images, pixels_per_view, epsilon, keys);
+    neglog_scale<<<grid, kThreads, 0, s>>>(images, pixels_per_view, n_views, keys);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        drr::set_last_error(std::string("drr_neglog_noalloc: launch: ") + cudaGetErrorString(e));
         return DRR_ERR_CUDA;
     }
     return DRR_OK;

@@ -113,6 +113,18 @@ drr_status drr_project(drr_volset *set, const drr_tables *tables, const drr_proj
  * scratch (cudaMallocAsync). */
 drr_status drr_neglog(float *images, int32_t n_views, int64_t pixels_per_view, float epsilon, void *stream);
 
+/* drr_neglog for callers that cannot allocate device memory. This entry point has no counterpart
+ * in the reference. Hosts that own the allocator and budget every byte up front, real-time loops
+ * in which cudaMalloc or cudaFree would stall the device, and pipelines that record their work
+ * into CUDA graphs while forbidding allocation calls all need a transform that allocates nothing.
+ * It computes exactly what drr_neglog computes but keeps its scratch (3 words per view) in one
+ * fixed device array inside the library, 48 KiB that every GPU loading the library keeps until the
+ * process exits; n_views above 4096 is rejected with DRR_ERR_UNSUPPORTED. The first call on a
+ * device looks up that array's device address (make it before any stream capture). All calls
+ * share the array: calls whose work overlaps on the GPU, on any streams, race and must be ordered
+ * by the caller. Each call resets the words it uses before reading them. */
+drr_status drr_neglog_noalloc(float *images, int32_t n_views, int64_t pixels_per_view, float epsilon, void *stream);
+
 /* In-place min(x, upper) over `n` floats: Projector(intensity_upper_bound=...), projector.py:697-698. */
 drr_status drr_clip_upper(float *images, int64_t n, float upper, void *stream);
 
