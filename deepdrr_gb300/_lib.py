@@ -26,11 +26,13 @@ DRR_MAX_MATERIALS = 16
 
 DRR_FLAG_ATTENUATE_OUTSIDE = 1 << 0
 DRR_FLAG_FULL_MARCH = 1 << 1
+DRR_FLAG_PERSISTENT = 1 << 2
 
 # Every symbol the header declares; the CPU test suite checks that the library exports all of them.
 EXPORTED_SYMBOLS = (
-    "drr_volset_create", "drr_volset_destroy", "drr_tables_create", "drr_tables_destroy",
-    "drr_project", "drr_neglog", "drr_neglog_noalloc", "drr_clip_upper", "drr_last_error", "drr_version",
+    "drr_volset_create", "drr_volset_destroy", "drr_volset_set_density", "drr_tables_create", "drr_tables_destroy",
+    "drr_project", "drr_project_adjoint", "drr_graph_create", "drr_graph_set_views", "drr_graph_launch", "drr_graph_destroy",
+    "drr_autotune", "drr_neglog", "drr_neglog_noalloc", "drr_clip_upper", "drr_last_error", "drr_version",
 )
 
 
@@ -62,6 +64,23 @@ class drr_project_args(ctypes.Structure):
         ("ijk_from_world", ctypes.c_void_p),
         ("intensity", ctypes.c_void_p), ("photon_prob", ctypes.c_void_p),
         ("area_density", ctypes.c_void_p), ("solid_angle", ctypes.c_void_p),
+        ("tile_warps_x", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32), ("items_per_grab", ctypes.c_int32),
+    ]
+
+
+class drr_adjoint_args(ctypes.Structure):
+    _fields_ = [
+        ("area_density", ctypes.c_void_p), ("grad_intensity", ctypes.c_void_p),
+        ("grad_photon_prob", ctypes.c_void_p), ("grad_area_density", ctypes.c_void_p),
+        ("grad_density", ctypes.c_void_p), ("grad_pose", ctypes.c_void_p),
+        ("center", ctypes.c_double * 3),
+    ]
+
+
+class drr_tune_result(ctypes.Structure):
+    _fields_ = [
+        ("tile_warps_x", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32), ("items_per_grab", ctypes.c_int32),
+        ("ms_per_view", ctypes.c_float),
     ]
 
 
@@ -88,12 +107,26 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     lib.drr_volset_create.restype = st
     lib.drr_volset_destroy.argtypes = [vp]
     lib.drr_volset_destroy.restype = st
+    lib.drr_volset_set_density.argtypes = [vp, i32, vp, vp]
+    lib.drr_volset_set_density.restype = st
     lib.drr_tables_create.argtypes = [vp, vp, vp, i32, i32, vp, ctypes.POINTER(vp)]
     lib.drr_tables_create.restype = st
     lib.drr_tables_destroy.argtypes = [vp]
     lib.drr_tables_destroy.restype = st
     lib.drr_project.argtypes = [vp, vp, ctypes.POINTER(drr_project_args), vp]
     lib.drr_project.restype = st
+    lib.drr_project_adjoint.argtypes = [vp, vp, ctypes.POINTER(drr_project_args), ctypes.POINTER(drr_adjoint_args), vp]
+    lib.drr_project_adjoint.restype = st
+    lib.drr_graph_create.argtypes = [vp, vp, ctypes.POINTER(drr_project_args), ctypes.POINTER(vp)]
+    lib.drr_graph_create.restype = st
+    lib.drr_graph_set_views.argtypes = [vp, vp, vp, vp]
+    lib.drr_graph_set_views.restype = st
+    lib.drr_graph_launch.argtypes = [vp, vp]
+    lib.drr_graph_launch.restype = st
+    lib.drr_graph_destroy.argtypes = [vp]
+    lib.drr_graph_destroy.restype = st
+    lib.drr_autotune.argtypes = [vp, vp, ctypes.POINTER(drr_project_args), i32, vp, ctypes.POINTER(drr_tune_result)]
+    lib.drr_autotune.restype = st
     lib.drr_neglog.argtypes = [vp, i32, ctypes.c_int64, ctypes.c_float, vp]
     lib.drr_neglog.restype = st
     lib.drr_neglog_noalloc.argtypes = [vp, i32, ctypes.c_int64, ctypes.c_float, vp]

@@ -1,11 +1,10 @@
-// drr_api.cu -- C ABI of libdrr_gb300.so: volume sets (textures), spectrum tables, projection.
+// drr_api.cu -- C ABI of libdrr_gb300.so: volume sets (textures, packed labels), spectrum tables.
 //
 // Host-side replacement for deepdrr/projector/projector.py (deepdrr v1.2.2):
 //   create_cuda_texture            projector.py:116-257   -> make_texture()
 //   Projector.initialize (volumes) projector.py:1464-1546 -> drr_volset_create()
 //   Projector.initialize (tables)  projector.py:1659-1686 -> drr_tables_create()
-//   _update_object_locations       projector.py:802-831   -> pack_view()
-//   _render_single                 projector.py:709-800   -> drr_project()
+// Projection itself (_render_single, projector.py:709-800) is in drr_project.cu.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
@@ -18,34 +17,21 @@
 
 #include "../../include/drr_gb300.h"
 #include "drr_forward.cuh"
+#include "drr_internal.h"
 
 namespace {
 
 thread_local std::string g_last_error;
 
-drr_status fail(drr_status s, const std::string &msg) {
-    g_last_error = msg;
-    return s;
-}
-
-drr_status cuda_fail(cudaError_t e, const char *what) {
-    g_last_error = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
-    return e == cudaErrorMemoryAllocation ? DRR_ERR_OUT_OF_MEMORY : DRR_ERR_CUDA;
-}
-
-#define DRR_CUDA_TRY(expr, what)                 \
-    do {                                         \
-        cudaError_t e_ = (expr);                 \
-        if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+#define DRR_CUDA_TRY(expr, what)                                \
+    do {                                                        \
+        cudaError_t e_ = (expr);                                \
+        if (e_ != cudaSuccess) return drr::cuda_fail(e_, what); \
     } while (0)
 
-struct Volume {
-    cudaArray_t density_array = nullptr;
-    cudaTextureObject_t density_tex = 0;
-    uint32_t *packed = nullptr;   // [(nk+1)][(nj+1)][(ni+1)] 2x2x2 label words
-    int ni = 0, nj = 0, nk = 0;
-    int density_type = DRR_DENSITY_F32;
-};
+using drr::cuda_fail;
+using drr::fail;
+using drr::Volume;
 
 // bfloat16 -> float16, exact for 0 and |x| in [2^-14, 65504]; anything else raises *bad.
 __global__ void bf16_to_f16_kernel(const __nv_bfloat16 *__restrict__ in, size_t n, __half *out, unsigned int *bad) {
@@ -108,6 +94,7 @@ drr_status make_texture(const void *src, int elem_bytes, cudaChannelFormatDesc f
 
 void free_volume(Volume &v) {
     if (v.density_tex) cudaDestroyTextureObject(v.density_tex);
+    if (v.density_point) cudaDestroyTextureObject(v.density_point);
     if (v.density_array) cudaFreeArray(v.density_array);
     if (v.packed) cudaFree(v.packed);
     v = Volume();
@@ -148,19 +135,43 @@ __global__ void pack_labels_kernel(const uint8_t *__restrict__ labels, int ni, i
 
 namespace drr {
 void set_last_error(const std::string &msg) { g_last_error = msg; }
+
+drr_status fail(drr_status s, const std::string &msg) {
+    g_last_error = msg;
+    return s;
+}
+
+drr_status cuda_fail(cudaError_t e, const char *what) {
+    g_last_error = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+    return e == cudaErrorMemoryAllocation ? DRR_ERR_OUT_OF_MEMORY : DRR_ERR_CUDA;
+}
+
+void free_staging(Staging &st) {
+    if (st.uploaded) {
+        cudaEventSynchronize(st.uploaded);
+        cudaEventDestroy(st.uploaded);
+    }
+    if (st.host) cudaFreeHost(st.host);
+    if (st.device) cudaFree(st.device);
+    if (st.counter) cudaFree(st.counter);
+    st = Staging();
+}
+
+drr_status ensure_staging(Staging &st, size_t bytes) {
+    if (!st.counter) DRR_CUDA_TRY(cudaMalloc(&st.counter, sizeof(unsigned int)), "cudaMalloc (work counter)");
+    if (!st.uploaded) DRR_CUDA_TRY(cudaEventCreateWithFlags(&st.uploaded, cudaEventDisableTiming), "cudaEventCreate");
+    if (bytes <= st.capacity) return DRR_OK;
+    if (st.pending) cudaEventSynchronize(st.uploaded);
+    if (st.host) cudaFreeHost(st.host);
+    if (st.device) cudaFree(st.device);
+    st.host = st.device = nullptr;
+    st.capacity = 0;
+    DRR_CUDA_TRY(cudaMallocHost(&st.host, bytes), "cudaMallocHost (view staging)");
+    DRR_CUDA_TRY(cudaMalloc(&st.device, bytes), "cudaMalloc (view records)");
+    st.capacity = bytes;
+    return DRR_OK;
+}
 }  // namespace drr
-
-struct drr_volset {
-    int n_volumes = 0;
-    int n_materials = 0;
-    Volume vol[DRR_MAX_VOLUMES];
-};
-
-struct drr_tables {
-    int n_bins = 0;
-    int n_materials = 0;
-    float *d_buf = nullptr;  // energies [n_bins] | pdf [n_bins] | mu [n_bins][n_materials]
-};
 
 extern "C" {
 
@@ -200,6 +211,11 @@ drr_status drr_volset_create(const drr_volume_desc *volumes, int32_t n_volumes, 
     if (!set) return fail(DRR_ERR_OUT_OF_MEMORY, "drr_volset_create: host allocation failed");
     set->n_volumes = n_volumes;
     set->n_materials = n_materials;
+    {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&set->sm_count, cudaDevAttrMultiProcessorCount, dev);
+    }
     unsigned int *d_max = nullptr;  // per-volume maximum label, then one range-violation flag
     cudaError_t e = cudaMalloc(&d_max, sizeof(unsigned int) * (DRR_MAX_VOLUMES + 1));
     if (e != cudaSuccess) {
@@ -287,7 +303,27 @@ drr_status drr_volset_destroy(drr_volset *set) {
     g_last_error.clear();
     if (!set) return DRR_OK;
     for (int i = 0; i < set->n_volumes; i++) free_volume(set->vol[i]);
+    drr::free_staging(set->staging);
     delete set;
+    return DRR_OK;
+}
+
+drr_status drr_volset_set_density(drr_volset *set, int32_t volume, const void *density, void *stream) {
+    g_last_error.clear();
+    if (!set || !density) return fail(DRR_ERR_INVALID_ARGUMENT, "drr_volset_set_density: NULL argument");
+    if (volume < 0 || volume >= set->n_volumes)
+        return fail(DRR_ERR_INVALID_ARGUMENT, "drr_volset_set_density: volume index out of range");
+    Volume &v = set->vol[volume];
+    if (v.density_type == DRR_DENSITY_BF16)
+        return fail(DRR_ERR_UNSUPPORTED, "drr_volset_set_density: bfloat16 volumes are converted once at creation");
+    const size_t elem = v.density_type == DRR_DENSITY_F32 ? 4 : 2;
+    cudaMemcpy3DParms cp;
+    std::memset(&cp, 0, sizeof(cp));
+    cp.srcPtr = make_cudaPitchedPtr(const_cast<void *>(density), (size_t)v.ni * elem, (size_t)v.ni, (size_t)v.nj);
+    cp.dstArray = v.density_array;
+    cp.extent = make_cudaExtent((size_t)v.ni, (size_t)v.nj, (size_t)v.nk);
+    cp.kind = cudaMemcpyDeviceToDevice;
+    DRR_CUDA_TRY(cudaMemcpy3DAsync(&cp, (cudaStream_t)stream), "drr_volset_set_density: cudaMemcpy3DAsync");
     return DRR_OK;
 }
 
@@ -338,140 +374,3 @@ drr_status drr_tables_destroy(drr_tables *tables) {
 
 }  // extern "C"
 
-namespace {
-
-// _update_object_locations (projector.py:802-831): float64 host geometry cast to float32. The
-// source position in IJK is computed in float64 in a fixed order, ((a0 s0 + a1 s1) + a2 s2) + a3.
-template <int NV>
-void pack_view(const drr_project_args &a, int nvol, int view, drr::ViewRec<NV> &rec) {
-    const double *W = a.world_from_index + (size_t)view * 9;
-    for (int j = 0; j < 9; j++) rec.w[j] = (float)W[j];
-    rec.pad = 0.0f;
-    const double *src = a.source_world + (size_t)view * 3;
-    for (int i = 0; i < NV; i++) {
-        drr::VolPose &vp = rec.vol[i];
-        if (i >= nvol) {
-            std::memset(&vp, 0, sizeof(vp));
-            continue;
-        }
-        const double *A = a.ijk_from_world + ((size_t)view * nvol + i) * 12;
-        for (int r = 0; r < 3; r++) {
-            for (int c = 0; c < 3; c++) vp.a[r * 3 + c] = (float)A[r * 4 + c];
-            volatile double acc = A[r * 4 + 0] * src[0];
-            acc = acc + A[r * 4 + 1] * src[1];
-            acc = acc + A[r * 4 + 2] * src[2];
-            acc = acc + A[r * 4 + 3];
-            vp.s[r] = (float)acc;
-        }
-    }
-}
-
-int material_bucket(int m) {
-    if (m <= 2) return 2;
-    if (m <= 3) return 3;
-    if (m <= 4) return 4;
-    if (m <= 6) return 6;
-    if (m <= 8) return 8;
-    return 16;
-}
-
-template <int NV>
-cudaError_t dispatch_m(const drr::ForwardParams<NV> &p, int bucket, cudaStream_t s) {
-    switch (bucket) {
-        case 2: return drr::launch_forward<NV, 2>(p, s);
-        case 3: return drr::launch_forward<NV, 3>(p, s);
-        case 4: return drr::launch_forward<NV, 4>(p, s);
-        case 6: return drr::launch_forward<NV, 6>(p, s);
-        case 8: return drr::launch_forward<NV, 8>(p, s);
-        default: return drr::launch_forward<NV, 16>(p, s);
-    }
-}
-
-template <int NV>
-drr_status project_nv(drr_volset *set, const drr_tables *tab, const drr_project_args &a, cudaStream_t s) {
-    drr::ForwardParams<NV> *pp = new (std::nothrow) drr::ForwardParams<NV>();
-    if (!pp) return fail(DRR_ERR_OUT_OF_MEMORY, "drr_project: host allocation failed");
-    drr::ForwardParams<NV> &p = *pp;
-    std::memset(&p, 0, sizeof(p));
-    for (int i = 0; i < NV; i++) {
-        const Volume &v = set->vol[i];
-        p.vol[i].density = v.density_tex;
-        p.vol[i].packed = v.packed;
-        p.vol[i].n[0] = v.ni;
-        p.vol[i].n[1] = v.nj;
-        p.vol[i].n[2] = v.nk;
-        p.vol[i].nm1[0] = (float)(v.ni - 1);
-        p.vol[i].nm1[1] = (float)(v.nj - 1);
-        p.vol[i].nm1[2] = (float)(v.nk - 1);
-        p.vol[i].hi[0] = (float)(v.ni - 0.5);
-        p.vol[i].hi[1] = (float)(v.nj - 0.5);
-        p.vol[i].hi[2] = (float)(v.nk - 0.5);
-        p.vol[i].priority = a.priority[i];
-        p.vol[i].enabled = a.enabled[i] ? 1 : 0;
-    }
-    p.energies = tab->d_buf;
-    p.pdf = tab->d_buf + tab->n_bins;
-    p.mu = tab->d_buf + 2 * tab->n_bins;
-    p.intensity = a.intensity;
-    p.photon_prob = a.photon_prob;
-    p.area_density = a.area_density;
-    p.solid_angle = a.solid_angle;
-    p.width = a.width;
-    p.height = a.height;
-    p.n_materials = set->n_materials;
-    p.n_bins = tab->n_bins;
-    p.step = a.step;
-    p.max_ray_length = a.max_ray_length;
-    p.attenuate = (a.flags & DRR_FLAG_ATTENUATE_OUTSIDE) ? 1 : 0;
-    p.air_index = a.air_index;
-    p.full_march = (a.flags & DRR_FLAG_FULL_MARCH) ? 1 : 0;
-    const int bucket = material_bucket(set->n_materials);
-    drr_status st = DRR_OK;
-    for (int v0 = 0; v0 < a.n_views; v0 += drr::kViewsPerLaunch) {
-        const int nv = a.n_views - v0 < drr::kViewsPerLaunch ? a.n_views - v0 : drr::kViewsPerLaunch;
-        p.view0 = v0;
-        p.n_views = nv;
-        for (int k = 0; k < nv; k++) pack_view<NV>(a, set->n_volumes, v0 + k, p.views[k]);
-        cudaError_t e = dispatch_m<NV>(p, bucket, s);
-        if (e != cudaSuccess) {
-            st = cuda_fail(e, "drr_project: kernel launch");
-            break;
-        }
-    }
-    delete pp;
-    return st;
-}
-
-}  // namespace
-
-extern "C" drr_status drr_project(drr_volset *set, const drr_tables *tables, const drr_project_args *args,
-                                  void *stream) {
-    g_last_error.clear();
-    if (!set || !tables || !args) return fail(DRR_ERR_INVALID_ARGUMENT, "drr_project: NULL handle or args");
-    const drr_project_args &a = *args;
-    if (a.width < 1 || a.height < 1) return fail(DRR_ERR_INVALID_ARGUMENT, "drr_project: empty detector");
-    if ((int64_t)a.width * a.height > (int64_t)1 << 28)
-        return fail(DRR_ERR_UNSUPPORTED, "drr_project: detector larger than 2^28 pixels");
-    if (a.height > 65535 * drr::kTileH) return fail(DRR_ERR_UNSUPPORTED, "drr_project: detector too tall");
-    if (a.n_views < 0) return fail(DRR_ERR_INVALID_ARGUMENT, "drr_project: n_views < 0");
-    if (a.n_views == 0) return DRR_OK;
-    if (!(a.step > 0.0f) || !std::isfinite(a.step))
-        return fail(DRR_ERR_INVALID_ARGUMENT, "drr_project: step must be a positive finite number");
-    if (!a.priority || !a.enabled || !a.world_from_index || !a.source_world || !a.ijk_from_world)
-        return fail(DRR_ERR_INVALID_ARGUMENT, "drr_project: NULL geometry pointer");
-    if (!a.intensity || !a.photon_prob) return fail(DRR_ERR_INVALID_ARGUMENT, "drr_project: NULL output pointer");
-    if (tables->n_materials != set->n_materials)
-        return fail(DRR_ERR_INVALID_ARGUMENT, "drr_project: tables and volume set disagree on n_materials");
-    for (int i = 0; i < set->n_volumes; i++)
-        if (a.priority[i] < 0 || a.priority[i] >= set->n_volumes)
-            return fail(DRR_ERR_INVALID_ARGUMENT, "drr_project: priority outside [0, n_volumes)");
-    if ((a.flags & DRR_FLAG_ATTENUATE_OUTSIDE) && (a.air_index < 0 || a.air_index >= set->n_materials))
-        return fail(DRR_ERR_INVALID_ARGUMENT, "drr_project: air_index outside [0, n_materials)");
-    cudaStream_t s = (cudaStream_t)stream;
-    switch (set->n_volumes) {
-        case 1: return project_nv<1>(set, tables, a, s);
-        case 2: return project_nv<2>(set, tables, a, s);
-        case 3: return project_nv<3>(set, tables, a, s);
-        default: return project_nv<4>(set, tables, a, s);
-    }
-}

@@ -74,8 +74,9 @@ struct ViewRec {
     VolPose vol[NV];
 };
 
+// Everything a ray needs except its view.
 template <int NV>
-struct ForwardParams {
+struct SceneParams {
     VolConst vol[NV];
     const float *energies;  // [n_bins] keV
     const float *pdf;       // [n_bins]
@@ -88,9 +89,29 @@ struct ForwardParams {
     float step, max_ray_length;
     int32_t attenuate, air_index;
     int32_t full_march;
+};
+
+// One launch of the plain kernel: up to kViewsPerLaunch views in the kernel parameters, one block
+// per 16 x 8 pixel tile, blockIdx.z = view.
+template <int NV>
+struct ForwardParams {
+    SceneParams<NV> s;
     int32_t view0;    // output index of views[0]
     int32_t n_views;  // views in this launch
     ViewRec<NV> views[kViewsPerLaunch];
+};
+
+// One launch of the persistent kernel: any number of views in device memory; resident blocks take
+// (view, tile) work items from an atomic counter until none are left.
+template <int NV>
+struct PersistentParams {
+    SceneParams<NV> s;
+    const ViewRec<NV> *views;  // device [n_views]
+    int32_t n_views;
+    int32_t tiles_x, tiles_y;  // tiles per view
+    int32_t warps_x;           // 1, 2 or 4 warps across a tile; a tile is (8 warps_x) x (16 / warps_x) pixels
+    int32_t items_per_grab;    // tiles taken per counter increment
+    unsigned int *counter;     // zero at launch
 };
 
 // ---- float32 groupings of the reference's dot products (see the file comment) ----------------
@@ -224,15 +245,10 @@ __device__ __forceinline__ float load_ad(const float ad[M], int m_sel) {
     return r;
 }
 
+// The whole computation of one ray: pixel (u, v) of `view`, written to output view `vout`.
 template <int NV, int M>
-__global__ void __launch_bounds__(kBlockThreads) forward_kernel(const __grid_constant__ ForwardParams<NV> p) {
-    const int lane = threadIdx.x & 31;
-    const int warp = threadIdx.x >> 5;
-    const int u = blockIdx.x * kTileW + ((warp & 1) << 3) + (lane & 7);
-    const int v = blockIdx.y * kTileH + ((warp >> 1) << 2) + (lane >> 3);
-    const int zv = blockIdx.z;
-    if (u >= p.width || v >= p.height || zv >= p.n_views) return;
-    const ViewRec<NV> &view = p.views[zv];
+__device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewRec<NV> &view, int u, int v,
+                                           size_t vout) {
     const float step = p.step;
     const int nmat = p.n_materials;
 
@@ -291,7 +307,6 @@ __global__ void __launch_bounds__(kBlockThreads) forward_kernel(const __grid_con
     }
     const float span_steps = ceilf(__fdiv_rn(__fsub_rn(maxA, minA), step));
     const size_t plane = (size_t)p.width * (size_t)p.height;
-    const size_t vout = (size_t)(p.view0 + zv);
     const size_t pix = (size_t)v * (size_t)p.width + (size_t)u;
     if (span_steps > (float)kMaxSteps || span_steps != span_steps) {
         // Only non-finite or absurd geometry gets here; report NaN rather than march for ever.
@@ -502,6 +517,50 @@ __global__ void __launch_bounds__(kBlockThreads) forward_kernel(const __grid_con
     if (p.solid_angle != nullptr) p.solid_angle[vout * plane + pix] = pixel_solid_angle(view.w, u, v);
 }
 
+// Plain launch: one block per 16 x 8 pixel tile (each warp an 8 x 4 pixel sub-tile), z = view.
+template <int NV, int M>
+__global__ void __launch_bounds__(kBlockThreads) forward_kernel(const __grid_constant__ ForwardParams<NV> p) {
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int u = blockIdx.x * kTileW + ((warp & 1) << 3) + (lane & 7);
+    const int v = blockIdx.y * kTileH + ((warp >> 1) << 2) + (lane >> 3);
+    const int zv = blockIdx.z;
+    if (u >= p.s.width || v >= p.s.height || zv >= p.n_views) return;
+    render_ray<NV, M>(p.s, p.views[zv], u, v, (size_t)(p.view0 + zv));
+}
+
+// Persistent launch: resident blocks take items_per_grab consecutive (view, tile) items at a time
+// from an atomic counter, view-major so that neighbouring blocks share a view's part of the volume
+// in L2. Rays of uneven length therefore balance across the GPU. Every block ends once the counter
+// passes the last item; the loop has no waits.
+template <int NV, int M>
+__global__ void __launch_bounds__(kBlockThreads) forward_persistent_kernel(const __grid_constant__ PersistentParams<NV> p) {
+    __shared__ unsigned int s_first;
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int wx = p.warps_x;
+    const int tile_w = 8 * wx, tile_h = 4 * (4 / wx);
+    const unsigned int per_view = (unsigned int)p.tiles_x * (unsigned int)p.tiles_y;
+    const unsigned int total = per_view * (unsigned int)p.n_views;
+    const unsigned int grab = (unsigned int)p.items_per_grab;
+    const int du = (warp % wx) * 8 + (lane & 7);
+    const int dv = (warp / wx) * 4 + (lane >> 3);
+    for (;;) {
+        if (threadIdx.x == 0) s_first = atomicAdd(p.counter, grab);
+        __syncthreads();
+        const unsigned int first = s_first;
+        __syncthreads();
+        if (first >= total) break;
+        const unsigned int last = first + grab < total ? first + grab : total;
+        for (unsigned int it = first; it < last; ++it) {
+            const unsigned int view = it / per_view, tile = it - view * per_view;
+            const int u = (int)(tile % (unsigned int)p.tiles_x) * tile_w + du;
+            const int v = (int)(tile / (unsigned int)p.tiles_x) * tile_h + dv;
+            if (u < p.s.width && v < p.s.height) render_ray<NV, M>(p.s, p.views[view], u, v, (size_t)view);
+        }
+    }
+}
+
 // Packs the labels of every 2x2x2 neighbourhood: word(b) for base b in [-1, n-1]^3 holds the labels
 // at clamp(b + d, 0, n - 1), corner c = dx | dy << 1 | dz << 2 in bits 4c..4c+3.
 __global__ void pack_labels_kernel(const uint8_t *__restrict__ labels, int ni, int nj, int nk, uint32_t *packed);
@@ -509,5 +568,9 @@ __global__ void pack_labels_kernel(const uint8_t *__restrict__ labels, int ni, i
 // Host-side launcher, explicitly instantiated per (NV, M) in drr_inst_nv*.cu.
 template <int NV, int M>
 cudaError_t launch_forward(const ForwardParams<NV> &p, cudaStream_t stream);
+template <int NV, int M>
+cudaError_t launch_persistent(const PersistentParams<NV> &p, int grid_blocks, cudaStream_t stream);
+template <int NV, int M>
+int persistent_occupancy();
 
 }  // namespace drr

@@ -1,5 +1,5 @@
-// drr_launch.cuh -- launcher template for the forward kernel; each drr_inst_nv*.cu instantiates it
-// for one volume count and every material bucket, so the instantiations compile in parallel.
+// drr_launch.cuh -- launcher templates for the forward kernels; each drr_inst_nv*.cu instantiates
+// them for one volume count and every material bucket, so the instantiations compile in parallel.
 #pragma once
 
 #include "drr_forward.cuh"
@@ -8,19 +8,40 @@ namespace drr {
 
 template <int NV, int M>
 cudaError_t launch_forward(const ForwardParams<NV> &p, cudaStream_t stream) {
-    dim3 grid((p.width + kTileW - 1) / kTileW, (p.height + kTileH - 1) / kTileH, p.n_views);
+    dim3 grid((p.s.width + kTileW - 1) / kTileW, (p.s.height + kTileH - 1) / kTileH, p.n_views);
     forward_kernel<NV, M><<<grid, kBlockThreads, 0, stream>>>(p);
     return cudaGetLastError();
 }
 
+template <int NV, int M>
+cudaError_t launch_persistent(const PersistentParams<NV> &p, int grid_blocks, cudaStream_t stream) {
+    forward_persistent_kernel<NV, M><<<grid_blocks, kBlockThreads, 0, stream>>>(p);
+    return cudaGetLastError();
+}
+
+// Resident blocks per SM of the persistent kernel (0 on error).
+template <int NV, int M>
+int persistent_occupancy() {
+    int blocks = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, forward_persistent_kernel<NV, M>, kBlockThreads, 0) !=
+        cudaSuccess)
+        return 0;
+    return blocks;
+}
+
 }  // namespace drr
 
-#define DRR_INSTANTIATE_FORWARD(NV)                                                             \
-    namespace drr {                                                                             \
-    template cudaError_t launch_forward<NV, 2>(const ForwardParams<NV> &, cudaStream_t);        \
-    template cudaError_t launch_forward<NV, 3>(const ForwardParams<NV> &, cudaStream_t);        \
-    template cudaError_t launch_forward<NV, 4>(const ForwardParams<NV> &, cudaStream_t);        \
-    template cudaError_t launch_forward<NV, 6>(const ForwardParams<NV> &, cudaStream_t);        \
-    template cudaError_t launch_forward<NV, 8>(const ForwardParams<NV> &, cudaStream_t);        \
-    template cudaError_t launch_forward<NV, 16>(const ForwardParams<NV> &, cudaStream_t);       \
+#define DRR_INSTANTIATE_ONE(NV, M)                                                                  \
+    template cudaError_t launch_forward<NV, M>(const ForwardParams<NV> &, cudaStream_t);            \
+    template cudaError_t launch_persistent<NV, M>(const PersistentParams<NV> &, int, cudaStream_t); \
+    template int persistent_occupancy<NV, M>();
+
+#define DRR_INSTANTIATE_FORWARD(NV) \
+    namespace drr {                 \
+    DRR_INSTANTIATE_ONE(NV, 2)      \
+    DRR_INSTANTIATE_ONE(NV, 3)      \
+    DRR_INSTANTIATE_ONE(NV, 4)      \
+    DRR_INSTANTIATE_ONE(NV, 6)      \
+    DRR_INSTANTIATE_ONE(NV, 8)      \
+    DRR_INSTANTIATE_ONE(NV, 16)     \
     }

@@ -214,3 +214,34 @@ def workload_ct(seed: int = 0, views: int = 32, shape=(512, 512, 400), sensor=(1
                          source_to_detector_distance=1020.0, pixel_size=pixel, sensor_size=sensor,
                          fraction_range=(0.5, 0.9))
     return [vol], projs, dict(step=0.1, spectrum=spectrum, neglog=True)
+
+
+def workload_multi(seed: int = 0, views: int = 256, sensor=(384, 384), pixel: float = 0.3,
+                   ct_shape=(512, 512, 400)):
+    """Three overlapping volumes of uneven size, each with its own seeded rigid pose: the CT phantom
+    (512 x 512 x 400), a 256^3 phantom at 1 mm and a 96 x 96 x 64 titanium implant mask; `views`
+    seeded poses on a 384^2 detector at 0.3 mm, 90 kVp (M = 4)."""
+    rng = np.random.default_rng(seed + 100)
+    hu, masks = ct_phantom(ct_shape, (0.8, 0.8, 1.0), seed)
+    ct = volume_from_hu(hu, spacing=(0.8, 0.8, 1.0), masks=masks)
+    ph = volume_from_hu(simple_phantom_hu(256, seed=seed + 1), spacing=(1.0, 1.0, 1.0))
+    ph.world_from_anatomical = random_rigid(rng, 40.0, 20.0)
+    imp = implant_volume((96, 96, 64), seed=seed + 2)
+    imp.world_from_anatomical = random_rigid(rng, 30.0, 45.0)
+    projs = random_views(views, ct.center_in_world, seed=seed + 3, sphere_mm=100.0, cone_deg=30.0,
+                         source_to_detector_distance=1020.0, pixel_size=pixel, sensor_size=sensor,
+                         fraction_range=(0.5, 0.9))
+    return [ct, ph, imp], projs, dict(step=0.1, spectrum="90KV_AL40", neglog=True)
+
+
+def workload_adjoint(seed: int = 0, views: int = 64, n: int = 256, sensor=(256, 256), pixel: float = 2.0):
+    """2D/3D registration case: the n^3 phantom at 1 mm (M = 3), `views` seeded poses on a 256^2
+    detector at 2 mm (magnification 2), 90 kVp, and a target pose (t in mm, rotation vector in
+    rad) perturbed by up to 5 mm and 5 degrees per axis."""
+    rng = np.random.default_rng(seed + 200)
+    vol = volume_from_hu(simple_phantom_hu(n, seed=seed), spacing=(1.0, 1.0, 1.0))
+    projs = random_views(views, vol.center_in_world, seed=seed + 4, sphere_mm=5.0, cone_deg=60.0,
+                         source_to_detector_distance=1020.0, pixel_size=pixel, sensor_size=sensor,
+                         fraction_range=(0.5, 0.5))
+    target = np.concatenate([rng.uniform(-5.0, 5.0, 3), np.deg2rad(rng.uniform(-5.0, 5.0, 3))])
+    return [vol], projs, dict(step=0.1, spectrum="90KV_AL40", neglog=False, target_pose=target)

@@ -18,6 +18,7 @@ import ctypes
 import logging
 import math
 import warnings
+from pathlib import Path
 from typing import List, Optional, Sequence, Union
 
 import numpy as np
@@ -279,38 +280,46 @@ class Projector:
             self.max_ray_length = self.source_to_detector_distance * 4
         return camera_projections
 
-    def project_tensors(self, *camera_projections, area_density: bool = False, solid_angle: bool = False,
-                        flags: int = 0, stream=None) -> dict:
-        """Render all views in one library call and keep the results on the GPU.
-
-        Returns torch tensors: ``intensity`` and ``photon_prob`` [N, H, W] (float32), and
-        optionally ``area_density`` [N, M, H, W] (g/cm^2) and ``solid_angle`` [N, H, W]."""
-        import torch
-
-        camera_projections = self._prepare_project(camera_projections)
+    def _geometry(self, camera_projections, ijk_from_world=None):
+        """float64 geometry arrays of the views (world_from_index, source, IJK_from_world). An
+        ``ijk_from_world`` array [n_volumes][3][4] (or [n_views][n_volumes][3][4]) replaces the
+        volumes' own poses."""
         views = [geo.view_arrays(p) for p in camera_projections]
         W0, H0 = views[0][2], views[0][3]
         if any((w, h) != (W0, H0) for _, _, w, h in views):
             raise ValueError("all views of one call must share the sensor size")
         n = len(views)
-        nv = len(self.volumes)
         wfi = np.ascontiguousarray(np.stack([v[0] for v in views]), dtype=np.float64)
         src = np.ascontiguousarray(np.stack([v[1] for v in views]), dtype=np.float64)
-        ijk = np.empty((n, nv, 3, 4), dtype=np.float64)
-        for i, vol in enumerate(self.volumes):
-            ijk[:, i] = np.asarray(vol.ijk_from_world.data[:3, :4])
+        ijk = np.empty((n, len(self.volumes), 3, 4), dtype=np.float64)
+        if ijk_from_world is not None:
+            ijk[:] = np.asarray(ijk_from_world, dtype=np.float64)[..., :3, :4]
+        else:
+            for i, vol in enumerate(self.volumes):
+                ijk[:, i] = np.asarray(vol.ijk_from_world.data[:3, :4])
+        return W0, H0, wfi, src, ijk
+
+    def _args(self, camera_projections, area_density, solid_angle, flags, launch, keep, ijk_from_world=None,
+              outputs: bool = True):
+        """drr_project_args for the views plus freshly allocated output tensors (none with
+        ``outputs`` False). Every array the args point to is appended to `keep`."""
+        import torch
+
+        W0, H0, wfi, src, ijk = self._geometry(camera_projections, ijk_from_world)
+        n = wfi.shape[0]
         prio = np.asarray(self.priorities, dtype=np.int32)
         enabled = np.asarray([1 if v.enabled else 0 for v in self.volumes], dtype=np.int32)
+        keep += [wfi, src, ijk, prio, enabled]
         dev = self.torch_device
         M = len(self.all_materials)
-        out = {
-            "intensity": torch.empty((n, H0, W0), dtype=torch.float32, device=dev),
-            "photon_prob": torch.empty((n, H0, W0), dtype=torch.float32, device=dev),
-        }
-        if area_density:
-            out["area_density"] = torch.empty((n, M, H0, W0), dtype=torch.float32, device=dev)
-        if solid_angle or self.collected_energy:
-            out["solid_angle"] = torch.empty((n, H0, W0), dtype=torch.float32, device=dev)
+        out = {}
+        if outputs:
+            out["intensity"] = torch.empty((n, H0, W0), dtype=torch.float32, device=dev)
+            out["photon_prob"] = torch.empty((n, H0, W0), dtype=torch.float32, device=dev)
+            if area_density:
+                out["area_density"] = torch.empty((n, M, H0, W0), dtype=torch.float32, device=dev)
+            if solid_angle or self.collected_energy:
+                out["solid_angle"] = torch.empty((n, H0, W0), dtype=torch.float32, device=dev)
         a = _lib.drr_project_args()
         a.width, a.height = W0, H0
         a.step = self.step
@@ -323,15 +332,156 @@ class Projector:
         a.world_from_index = wfi.ctypes.data
         a.source_world = src.ctypes.data
         a.ijk_from_world = ijk.ctypes.data
-        a.intensity = out["intensity"].data_ptr()
-        a.photon_prob = out["photon_prob"].data_ptr()
+        a.intensity = out["intensity"].data_ptr() if outputs else None
+        a.photon_prob = out["photon_prob"].data_ptr() if outputs else None
         a.area_density = out["area_density"].data_ptr() if "area_density" in out else None
         a.solid_angle = out["solid_angle"].data_ptr() if "solid_angle" in out else None
-        s = stream if stream is not None else torch.cuda.current_stream(dev)
-        _lib.check(_lib.load().drr_project(self._volset, self._tables, ctypes.byref(a),
-                                           ctypes.c_void_p(s.cuda_stream)))
+        if launch:
+            a.tile_warps_x = int(launch.get("tile_warps_x", 0))
+            a.blocks_per_sm = int(launch.get("blocks_per_sm", 0))
+            a.items_per_grab = int(launch.get("items_per_grab", 0))
         self.output_shape = (W0, H0)
+        return a, out
+
+    def _stream_ptr(self, stream):
+        import torch
+
+        s = stream if stream is not None else torch.cuda.current_stream(self.torch_device)
+        return ctypes.c_void_p(s.cuda_stream)
+
+    def project_tensors(self, *camera_projections, area_density: bool = False, solid_angle: bool = False,
+                        flags: int = 0, stream=None, persistent: bool = False, launch: Optional[dict] = None,
+                        ijk_from_world=None) -> dict:
+        """Render all views in one library call and keep the results on the GPU.
+
+        ``persistent`` renders every view in one persistent launch (dynamic scheduling of (view,
+        tile) items); ``launch`` sets its shape (keys tile_warps_x, blocks_per_sm, items_per_grab,
+        e.g. from :meth:`autotune`). Returns torch tensors: ``intensity`` and ``photon_prob``
+        [N, H, W] (float32), and optionally ``area_density`` [N, M, H, W] (g/cm^2) and
+        ``solid_angle`` [N, H, W]. ``ijk_from_world`` ([n_volumes][3][4], float64) replaces the
+        volumes' poses for this call."""
+        camera_projections = self._prepare_project(camera_projections)
+        keep = []
+        a, out = self._args(camera_projections, area_density, solid_angle,
+                            flags | (_lib.DRR_FLAG_PERSISTENT if persistent else 0), launch, keep, ijk_from_world)
+        _lib.check(_lib.load().drr_project(self._volset, self._tables, ctypes.byref(a), self._stream_ptr(stream)))
         return out
+
+    def set_density(self, density, volume: int = 0, stream=None) -> None:
+        """Replace the densities of one volume from a CUDA tensor [ni, nj, nk] (the reference's
+        layout), keeping its labels; float32 and float16 volumes."""
+        import torch
+
+        if not self.initialized:
+            raise RuntimeError("Projector has not been initialized.")
+        ni, nj, nk = self.volumes[volume].shape
+        if tuple(density.shape) != (ni, nj, nk):
+            raise ValueError(f"density shape {tuple(density.shape)} != volume shape {(ni, nj, nk)}")
+        dt = {"float32": torch.float32, "float16": torch.float16}.get(self.density_dtype)
+        if dt is None:
+            raise ValueError("set_density supports float32 and float16 volumes")
+        dens = density.detach().to(device=self.torch_device, dtype=dt).permute(2, 1, 0).contiguous()
+        s = stream if stream is not None else torch.cuda.current_stream(self.torch_device)
+        _lib.check(_lib.load().drr_volset_set_density(self._volset, int(volume), dens.data_ptr(),
+                                                      ctypes.c_void_p(s.cuda_stream)))
+        dens.record_stream(s)
+
+    def project_adjoint(self, *camera_projections, area_density=None, grad_intensity=None, grad_photon_prob=None,
+                        grad_area_density=None, density: bool = True, pose: bool = False, center=None,
+                        ijk_from_world=None, stream=None) -> dict:
+        """Gradients of a loss through :meth:`project_tensors` (one volume, no air attenuation).
+
+        Upstream gradients are CUDA tensors shaped like the forward's outputs; ``area_density`` is
+        the forward's [N, M, H, W] output for the same views (None: recomputed). Returns
+        ``density``: dL/d(density) [ni, nj, nk] float32, and with ``pose`` ``pose``: [N, 6]
+        dL/d(translation, rotation vector) of a rigid motion of the volume about ``center``
+        (world, default the volume's centre), per view."""
+        import torch
+
+        camera_projections = self._prepare_project(camera_projections)
+        keep = []
+        a, _ = self._args(camera_projections, False, False, 0, None, keep, ijk_from_world, outputs=False)
+        n = a.n_views
+        ni, nj, nk = self.volumes[0].shape
+        dev = self.torch_device
+        out = {}
+        adj = _lib.drr_adjoint_args()
+
+        def ptr(t, name):
+            if t is None:
+                return None
+            if not (t.is_cuda and t.dtype == torch.float32 and t.is_contiguous()):
+                raise ValueError(f"{name} must be a contiguous float32 CUDA tensor")
+            keep.append(t)
+            return t.data_ptr()
+
+        adj.area_density = ptr(area_density, "area_density")
+        adj.grad_intensity = ptr(grad_intensity, "grad_intensity")
+        adj.grad_photon_prob = ptr(grad_photon_prob, "grad_photon_prob")
+        adj.grad_area_density = ptr(grad_area_density, "grad_area_density")
+        if density:
+            out["density"] = torch.zeros((nk, nj, ni), dtype=torch.float32, device=dev)
+            adj.grad_density = out["density"].data_ptr()
+        if pose:
+            out["pose"] = torch.zeros((n, 6), dtype=torch.float32, device=dev)
+            adj.grad_pose = out["pose"].data_ptr()
+        c = self.volume_center_world(0) if center is None else np.asarray(center, dtype=np.float64)
+        for k in range(3):
+            adj.center[k] = float(c[k])
+        _lib.check(_lib.load().drr_project_adjoint(self._volset, self._tables, ctypes.byref(a), ctypes.byref(adj),
+                                                   self._stream_ptr(stream)))
+        if density:
+            out["density"] = out["density"].permute(2, 1, 0)
+        return out
+
+    def volume_center_world(self, volume: int = 0) -> np.ndarray:
+        """World position of the centre of a volume's voxel grid."""
+        v = self.volumes[volume]
+        ijk = (np.asarray(v.shape, dtype=np.float64) - 1.0) / 2.0
+        wfi = np.linalg.inv(np.asarray(v.ijk_from_world.data, dtype=np.float64))
+        return (wfi @ np.append(ijk, 1.0))[:3]
+
+    def autotune(self, *camera_projections, max_views: int = 32, stream=None, cache: bool = True) -> dict:
+        """Fastest persistent launch shape for these views (cached per GPU, volumes, materials,
+        detector size and view count in ~/.cache/deepdrr_gb300/autotune.json)."""
+        import json
+        import os
+        import torch
+
+        camera_projections = self._prepare_project(camera_projections)
+        W0, H0 = geo.view_arrays(camera_projections[0])[2:]
+        key = "|".join(str(x) for x in (torch.cuda.get_device_name(self.torch_device),
+                                          [v.shape for v in self.volumes], len(self.all_materials), W0, H0,
+                                          min(len(camera_projections), max_views), self.density_dtype))
+        path = Path(os.environ.get("DEEPDRR_GB300_CACHE", Path.home() / ".cache" / "deepdrr_gb300")) / "autotune.json"
+        table = {}
+        if cache and path.exists():
+            try:
+                table = json.loads(path.read_text())
+            except (OSError, ValueError):
+                table = {}
+        if key in table:
+            return table[key]
+        keep = []
+        a, _ = self._args(camera_projections, False, False, _lib.DRR_FLAG_PERSISTENT, None, keep)
+        r = _lib.drr_tune_result()
+        _lib.check(_lib.load().drr_autotune(self._volset, self._tables, ctypes.byref(a), int(max_views),
+                                            self._stream_ptr(stream), ctypes.byref(r)))
+        best = dict(tile_warps_x=r.tile_warps_x, blocks_per_sm=r.blocks_per_sm, items_per_grab=r.items_per_grab,
+                    ms_per_view=r.ms_per_view)
+        if cache:
+            table[key] = best
+            try:
+                path.parent.mkdir(parents=True, exist_ok=True)
+                path.write_text(json.dumps(table, indent=1))
+            except OSError:
+                pass
+        return best
+
+    def capture(self, *camera_projections, area_density: bool = False, launch: Optional[dict] = None) -> "ProjectionGraph":
+        """Capture a persistent projection of these views in a CUDA graph (see ProjectionGraph)."""
+        camera_projections = self._prepare_project(camera_projections)
+        return ProjectionGraph(self, camera_projections, area_density, launch)
 
     def project(self, *camera_projections) -> np.ndarray:
         """Render, post-process and return numpy float32 [H, W] (one view) or [N, H, W]."""
@@ -373,3 +523,44 @@ class Projector:
             out.append(e / (px * py))
         import torch
         return torch.stack(out)
+
+
+class ProjectionGraph:
+    """A persistent projection of a fixed number of views captured in a CUDA graph.
+
+    The graph holds the upload of the view records, the reset of the work counter and the
+    persistent kernel; ``launch()`` replays it into the same output tensors, ``set_views(...)``
+    replaces the view geometry (same number of views and sensor size) before the next replay.
+    """
+
+    def __init__(self, projector: Projector, camera_projections, area_density: bool, launch: Optional[dict]):
+        self.projector = projector
+        self._keep = []
+        self.args, self.outputs = projector._args(camera_projections, area_density, False,
+                                                  _lib.DRR_FLAG_PERSISTENT, launch, self._keep)
+        self.n_views = self.args.n_views
+        handle = ctypes.c_void_p()
+        _lib.check(_lib.load().drr_graph_create(projector._volset, projector._tables, ctypes.byref(self.args),
+                                                ctypes.byref(handle)))
+        self._graph = handle
+
+    def set_views(self, *camera_projections) -> None:
+        W0, H0, wfi, src, ijk = self.projector._geometry(camera_projections)
+        if wfi.shape[0] != self.n_views or (W0, H0) != (self.args.width, self.args.height):
+            raise ValueError("a captured projection keeps its number of views and sensor size")
+        _lib.check(_lib.load().drr_graph_set_views(self._graph, wfi.ctypes.data, src.ctypes.data, ijk.ctypes.data))
+
+    def launch(self, stream=None) -> dict:
+        _lib.check(_lib.load().drr_graph_launch(self._graph, self.projector._stream_ptr(stream)))
+        return self.outputs
+
+    def close(self) -> None:
+        if self._graph:
+            _lib.load().drr_graph_destroy(self._graph)
+            self._graph = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -69,6 +69,12 @@ drr_status drr_volset_create(const drr_volume_desc *volumes, int32_t n_volumes, 
                              void *stream, drr_volset **out);
 drr_status drr_volset_destroy(drr_volset *set);
 
+/* Replace the densities of volume `volume` from a device array of the type and size it was created
+ * with ([nk][nj][ni], i fastest), asynchronously on `stream` (float32 and float16 volumes; a
+ * bfloat16 volume returns DRR_ERR_UNSUPPORTED). Labels are kept. No counterpart in the reference:
+ * it lets a differentiable caller project the current iterate without rebuilding the set. */
+drr_status drr_volset_set_density(drr_volset *set, int32_t volume, const void *density, void *stream);
+
 /* Upload a spectrum and its mass-attenuation table. Host pointers:
  *   energies_kev [n_bins], pdf [n_bins], mu_over_rho [n_bins][n_materials] (cm^2/g).
  * Replaces projector.py:1659-1686. */
@@ -78,7 +84,8 @@ drr_status drr_tables_destroy(drr_tables *tables);
 
 enum {
     DRR_FLAG_ATTENUATE_OUTSIDE = 1 << 0, /* Projector(attenuate_outside_volume=True), project_kernel.cu:358-361,522-527,557-560 */
-    DRR_FLAG_FULL_MARCH = 1 << 1         /* march every step from minAlpha like the reference (no prefix skip); for testing */
+    DRR_FLAG_FULL_MARCH = 1 << 1,        /* march every step from minAlpha like the reference (no prefix skip); for testing */
+    DRR_FLAG_PERSISTENT = 1 << 2         /* one persistent launch for all views (dynamic (view, tile) scheduling) */
 };
 
 /* Arguments of one drr_project call: `n_views` views of the same volume set. */
@@ -100,11 +107,66 @@ typedef struct {
     float *area_density;            /* device [n_views][n_materials][H][W] in g/cm^2, or NULL */
     float *solid_angle;             /* device [n_views][H][W] pixel solid angles (sr), or NULL;
                                        project_kernel.cu:14-133 */
+    /* launch shape of DRR_FLAG_PERSISTENT (0 = default; drr_autotune picks them per workload) */
+    int32_t tile_warps_x;           /* 1, 2 or 4 warps across a tile of 4 warps (tiles 8x16, 16x8, 32x4) */
+    int32_t blocks_per_sm;          /* resident 128-thread blocks per SM */
+    int32_t items_per_grab;         /* tiles a block takes per atomic increment */
 } drr_project_args;
 
 /* Render `args->n_views` views into the caller's device buffers, asynchronously on `stream`.
- * Replaces projector.py:709-800 and the projectKernel launch (project_kernel.cu:135-650). */
+ * Replaces projector.py:709-800 and the projectKernel launch (project_kernel.cu:135-650).
+ * Without DRR_FLAG_PERSISTENT every group of 32 views is one launch with the geometry in the
+ * kernel parameters. With it, all views go into one persistent launch whose view records are
+ * staged through library-owned pinned and device buffers (one staging per volume set: calls on
+ * one volume set from several streams at once must be ordered by the caller). */
 drr_status drr_project(drr_volset *set, const drr_tables *tables, const drr_project_args *args, void *stream);
+
+/* A persistent projection captured in a CUDA graph (upload of the view records, reset of the work
+ * counter, kernel), replayed by drr_graph_launch. The output pointers, volume set, tables, sizes
+ * and launch shape of `args` are fixed at creation; the view geometry can be replaced between
+ * replays with drr_graph_set_views (same number of views). No counterpart in the reference: this
+ * replaces its serial loop over views (projector.py:679-685) for many views per call. */
+typedef struct drr_graph drr_graph;
+drr_status drr_graph_create(drr_volset *set, const drr_tables *tables, const drr_project_args *args,
+                            drr_graph **out);
+drr_status drr_graph_set_views(drr_graph *graph, const double *world_from_index, const double *source_world,
+                               const double *ijk_from_world);
+drr_status drr_graph_launch(drr_graph *graph, void *stream);
+drr_status drr_graph_destroy(drr_graph *graph);
+
+/* Launch-shape autotuner of the persistent projection: times candidate shapes on `args` (up to
+ * `max_views` of its views; the outputs are overwritten) on `stream` and returns the fastest.
+ * No counterpart in the reference. */
+typedef struct {
+    int32_t tile_warps_x;
+    int32_t blocks_per_sm;
+    int32_t items_per_grab;
+    float ms_per_view;
+} drr_tune_result;
+drr_status drr_autotune(drr_volset *set, const drr_tables *tables, const drr_project_args *args, int32_t max_views,
+                        void *stream, drr_tune_result *best);
+
+/* Upstream gradients and gradient outputs of drr_project_adjoint. Device pointers. */
+typedef struct {
+    const float *area_density;      /* [n_views][n_materials][H][W]: drr_project's area_density for the
+                                       same args, or NULL to recompute it (stream-ordered scratch) */
+    const float *grad_intensity;    /* [n_views][H][W] dL/d(intensity), or NULL */
+    const float *grad_photon_prob;  /* [n_views][H][W] dL/d(photon_prob), or NULL */
+    const float *grad_area_density; /* [n_views][n_materials][H][W] dL/d(area_density), or NULL */
+    float *grad_density;            /* [nk][nj][ni] dL/d(density), accumulated into; or NULL */
+    float *grad_pose;               /* [n_views][6] dL/d(translation xyz, rotation vector xyz) of a rigid
+                                       motion of the volume about `center` (world frame, at zero
+                                       motion), accumulated into; or NULL */
+    double center[3];               /* rotation centre, world */
+} drr_adjoint_args;
+
+/* Gradients of a loss through drr_project for one enabled volume without DRR_FLAG_ATTENUATE_OUTSIDE
+ * (else DRR_ERR_UNSUPPORTED). The density gradient is the exact adjoint of the kernel's samples,
+ * with the texture unit's 8-bit corner weights; the pose gradient differentiates the continuous
+ * trilinear interpolation of the same texels and labels, with the march's sample positions held
+ * fixed. No counterpart in the reference (its projector is not differentiable). */
+drr_status drr_project_adjoint(drr_volset *set, const drr_tables *tables, const drr_project_args *args,
+                               const drr_adjoint_args *adjoint, void *stream);
 
 /* In-place negative-log transform of `n_views` float32 images of `pixels_per_view` pixels each,
  * on `stream`: per view x += min(x) + epsilon; x = -log(x); x = (x - min) / (max - min), and every
