@@ -32,7 +32,7 @@ DRR_FLAG_PERSISTENT = 1 << 2
 EXPORTED_SYMBOLS = (
     "drr_volset_create", "drr_volset_destroy", "drr_volset_set_density", "drr_tables_create", "drr_tables_destroy",
     "drr_project", "drr_project_adjoint", "drr_graph_create", "drr_graph_set_views", "drr_graph_launch", "drr_graph_destroy",
-    "drr_autotune", "drr_neglog", "drr_neglog_noalloc", "drr_clip_upper", "drr_last_error", "drr_version",
+    "drr_autotune", "drr_add_noise", "drr_poisson_sample", "drr_neglog", "drr_neglog_noalloc", "drr_clip_upper", "drr_last_error", "drr_version",
 )
 
 
@@ -127,6 +127,10 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     lib.drr_graph_destroy.restype = st
     lib.drr_autotune.argtypes = [vp, vp, ctypes.POINTER(drr_project_args), i32, vp, ctypes.POINTER(drr_tune_result)]
     lib.drr_autotune.restype = st
+    lib.drr_add_noise.argtypes = [vp, vp, vp, i32, i32, i32, ctypes.c_double, ctypes.c_uint64, vp]
+    lib.drr_add_noise.restype = st
+    lib.drr_poisson_sample.argtypes = [vp, ctypes.c_int64, ctypes.c_uint64, vp, vp]
+    lib.drr_poisson_sample.restype = st
     lib.drr_neglog.argtypes = [vp, i32, ctypes.c_int64, ctypes.c_float, vp]
     lib.drr_neglog.restype = st
     lib.drr_neglog_noalloc.argtypes = [vp, i32, ctypes.c_int64, ctypes.c_float, vp]

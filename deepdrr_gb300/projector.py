@@ -497,12 +497,19 @@ class Projector:
         images = out["intensity"]
         if self.collected_energy:
             images = self._collected_energy(camera_projections, images, out["solid_angle"]).contiguous()
-        if self.add_noise:
-            raise NotImplementedError("Poisson noise is not implemented yet")
         lib = _lib.load()
         s = stream if stream is not None else torch.cuda.current_stream(self.torch_device)
         sp = ctypes.c_void_p(s.cuda_stream)
         n, h, w = images.shape
+        if self.add_noise:
+            # projector.py:691-695: shot noise from photon_prob * photon_count. The seed is drawn
+            # from numpy's global generator, which the reference's np.random.poisson also uses, so
+            # np.random.seed makes a run repeatable in the same way.
+            seed = int(np.random.randint(0, 2 ** 63 - 1, dtype=np.int64))
+            noisy = torch.empty_like(images)
+            _lib.check(lib.drr_add_noise(images.data_ptr(), out["photon_prob"].data_ptr(), noisy.data_ptr(), n, h, w,
+                                         float(self.photon_count), seed, sp))
+            images = noisy
         if self.intensity_upper_bound is not None:
             _lib.check(lib.drr_clip_upper(images.data_ptr(), images.numel(), float(self.intensity_upper_bound), sp))
         if self.neglog:

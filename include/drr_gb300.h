@@ -15,6 +15,12 @@
  *   drr_project         Projector._render_single + _update_object_locations + the projectKernel
  *                       launch, projector.py:709-800, 802-831; kernel deepdrr/projector/project_kernel.cu:135-650
  *   drr_*_destroy       Projector.free, projector.py:1719-1764
+ *   drr_add_noise       analytic_generators.add_noise, deepdrr/projector/analytic_generators.py:10-18
+ *   drr_clip_upper,     the post-processing of Projector.project, projector.py:697-702, and
+ *   drr_neglog          deepdrr/utils/image_utils.py:18-58
+ * and adds what the reference does not have: persistent multi-view launches, their CUDA-graph
+ * capture and launch-shape autotuner (drr_graph_*, drr_autotune), and the adjoint
+ * (drr_project_adjoint, drr_volset_set_density) for density and pose gradients.
  *
  * Conventions. Volumes are stored i-fastest ([nk][nj][ni]), i.e. the reference's
  * np.moveaxis(data, [0,1,2], [2,1,0]) layout (projector.py:1469). Images are row-major [H][W]
@@ -44,7 +50,8 @@ typedef enum {
 typedef enum {
     DRR_DENSITY_F32 = 0, /* float32 densities, hardware-filtered like the reference */
     DRR_DENSITY_F16 = 1, /* IEEE half densities, hardware-filtered, float32 accumulation */
-    DRR_DENSITY_BF16 = 2 /* bfloat16 densities, filtered in software, float32 accumulation */
+    DRR_DENSITY_BF16 = 2 /* bfloat16 densities, held exactly in a float16 texture (values 0 or with |x| in
+                            [2^-14, 65504]; others are rejected), float32 accumulation */
 } drr_density_type;
 
 #define DRR_MAX_VOLUMES 4
@@ -167,6 +174,23 @@ typedef struct {
  * fixed. No counterpart in the reference (its projector is not differentiable). */
 drr_status drr_project_adjoint(drr_volset *set, const drr_tables *tables, const drr_project_args *args,
                                const drr_adjoint_args *adjoint, void *stream);
+
+/* Detector noise of Projector(add_noise=True): replaces analytic_generators.add_noise
+ * (deepdrr/projector/analytic_generators.py:10-18, called at projector.py:691-695). For `n_views`
+ * [height][width] float32 images, lambda = photon_prob * photon_count (float32) and
+ *   out = clip(intensity + convolve2d((Poisson(lambda) - lambda) * intensity / lambda, K, "same"), 0, 1e31)
+ * with K the reference's 3x3 shot-noise kernel, zero fill at the borders, the arithmetic after the
+ * variate in float64 and the result rounded to float32. The reference's electronic-noise term has
+ * factor 0 and is not generated. Variates are Philox4x32-10 (key `seed`, counter = the pixel's flat
+ * index view * H * W + row * W + column) through inversion (lambda < 10) or Hoermann's PTRS, so a
+ * seed gives the same images on any launch shape. `out` must not alias the inputs; a pixel with
+ * photon_prob 0 gives NaN in its 3x3 neighbourhood, as in the reference (0 / 0). */
+drr_status drr_add_noise(const float *intensity, const float *photon_prob, float *out, int32_t n_views,
+                         int32_t height, int32_t width, double photon_count, uint64_t seed, void *stream);
+
+/* The variates drr_add_noise draws: out[i] = Poisson(lambda[i]) with counter i under key `seed`
+ * (float32, exact below 2^24; NaN for a negative or non-finite lambda). */
+drr_status drr_poisson_sample(const float *lambda, int64_t n, uint64_t seed, float *out, void *stream);
 
 /* In-place negative-log transform of `n_views` float32 images of `pixels_per_view` pixels each,
  * on `stream`: per view x += min(x) + epsilon; x = -log(x); x = (x - min) / (max - min), and every
