@@ -108,8 +108,10 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def workload(args, rank: int):
+def workload(args, rank: int, world: int = 1):
+    """The seeded workload; under N ranks each renders its own contiguous share of N x views poses."""
     from deepdrr_gb300 import phantoms
+    from deepdrr_gb300.replicas import shard
 
     if args.small:
         vols, projs, kw = phantoms.workload_simple(seed=args.seed, views=args.views)
@@ -118,13 +120,13 @@ def workload(args, rank: int):
         vols, projs, kw = phantoms.workload_multi(seed=args.seed + rank, views=args.views)
         name = f"multi3_ct512x512x400+256^3+96x96x64_det384_{args.views}views_90kV"
     elif args.workload == "ct512":
-        vols, projs, kw = phantoms.workload_ct(seed=args.seed, views=args.views * (rank + 1), shape=(512, 512, 512),
+        vols, projs, kw = phantoms.workload_ct(seed=args.seed, views=args.views * world, shape=(512, 512, 512),
                                                spectrum="120KV_AL43")
-        projs = projs[args.views * rank:]
+        projs = shard(projs, rank, world)
         name = f"ct512x512x512_det1536_{args.views}views_120kV"
     else:
-        vols, projs, kw = phantoms.workload_ct(seed=args.seed, views=args.views * (rank + 1))
-        projs = projs[args.views * rank:]
+        vols, projs, kw = phantoms.workload_ct(seed=args.seed, views=args.views * world)
+        projs = shard(projs, rank, world)
         name = f"ct512x512x400_det1536_{args.views}views_90kV"
     return vols, projs, kw, name
 
@@ -350,6 +352,7 @@ def main():
 
     import deepdrr_gb300 as dd
     from deepdrr_gb300 import metrics, tables
+    from deepdrr_gb300.replicas import max_over_ranks
 
     torch.cuda.set_device(local)
     dist = None
@@ -357,7 +360,7 @@ def main():
         import torch.distributed as dist
 
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    vols, projs, kw, name = workload(args, rank)
+    vols, projs, kw, name = workload(args, rank, world)
     src = tables.NpzTables(TABLES)
     nviews = len(projs)
     p = dd.Projector(vols, spectrum=kw["spectrum"], step=kw["step"], tables=src, neglog=True,
@@ -392,11 +395,7 @@ def main():
     e1.synchronize()
     clk = clocks.stop()
     barrier()
-    ms = e0.elapsed_time(e1)
-    if dist is not None:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(e0.elapsed_time(e1), device="cuda")
     ms_per_step = ms / args.steps
     value = nviews * world * args.steps / (ms / 1000.0)
     gsamples = samples_per_step * world * args.steps / (ms / 1000.0) / 1e9

@@ -49,10 +49,11 @@ struct AdjointParams {
 // Corner weights of the texture unit for the density coordinate x = p + 0.5 on one axis of n
 // texels: texel i0 = fix >> 8, fraction a = fix & 255 (see the oracle's tex_linear).
 __device__ __forceinline__ void hw_axis(float x, int n, int &i0, int &i1, int &a) {
-    // (x - 0.5) * 256 is exact wherever it is >= 0 (x * 256 is exact and 128 a multiple of its ulp);
+    // (x - 0.5) * 256 is exact wherever it is >= 0 (x * 256 is exact and 128 a multiple of its ulp,
+    // so the fused form rounds nothing there);
     // the clamp to [0, (n - 1) * 256] is the unit's own, and round-half-up is done without a
     // rounding addition.
-    float v = __fsub_rn(__fmul_rn(x, 256.0f), 128.0f);
+    float v = __fmaf_rn(x, 256.0f, -128.0f);
     v = fminf(fmaxf(v, 0.0f), (float)(n - 1) * 256.0f);
     const float fl = floorf(v);
     const int fix = (int)fl + (__fsub_rn(v, fl) >= 0.5f ? 1 : 0);
@@ -76,7 +77,31 @@ __device__ __forceinline__ void hw_weights(int Ax, int Ay, int Az, int W[8]) {
     }
 }
 
+// Material weight of each of the eight corners of a label word: gr[label of corner c].
 template <int M>
+__device__ __forceinline__ float gr_of(const float gr[M], int L) {
+    float v = 0.0f;
+#pragma unroll
+    for (int m = 0; m < M; m++)
+        if (m == L) v = gr[m];
+    return v;
+}
+
+// Trilinear gradient of eight corner values c = dx | dy << 1 | dz << 2 at fractions (fx, fy, fz).
+__device__ __forceinline__ void trilinear_grad(const float v[8], float fx, float fy, float fz, float gx, float gy,
+                                               float gz, float d[3]) {
+    d[0] = gz * (gy * (v[1] - v[0]) + fy * (v[3] - v[2])) + fz * (gy * (v[5] - v[4]) + fy * (v[7] - v[6]));
+    d[1] = gz * (gx * (v[2] - v[0]) + fx * (v[3] - v[1])) + fz * (gx * (v[6] - v[4]) + fx * (v[7] - v[5]));
+    d[2] = gy * (gx * (v[4] - v[0]) + fx * (v[5] - v[1])) + fy * (gx * (v[6] - v[2]) + fx * (v[7] - v[3]));
+}
+
+__device__ __forceinline__ float trilinear(const float v[8], float fx, float fy, float fz, float gx, float gy,
+                                           float gz) {
+    return gz * (gy * (gx * v[0] + fx * v[1]) + fy * (gx * v[2] + fx * v[3])) +
+           fz * (gy * (gx * v[4] + fx * v[5]) + fy * (gx * v[6] + fx * v[7]));
+}
+
+template <int M, bool POSE>
 __global__ void __launch_bounds__(kBlockThreads) adjoint_kernel(const __grid_constant__ AdjointParams P) {
     const SceneParams<1> &p = P.s;
     const int lane = threadIdx.x & 31;
@@ -105,20 +130,26 @@ __global__ void __launch_bounds__(kBlockThreads) adjoint_kernel(const __grid_con
         }
         const float gI = P.grad_intensity ? P.grad_intensity[zv * plane + pix] : 0.0f;
         const float gP = P.grad_photon_prob ? P.grad_photon_prob[zv * plane + pix] : 0.0f;
-        for (int bin = 0; bin < p.n_bins; bin++) {
-            float x = 0.0f;
+        if (gI != 0.0f || gP != 0.0f) {
+            for (int bin = 0; bin < p.n_bins; bin++) {
+                float x = 0.0f;
 #pragma unroll
-            for (int m = 0; m < M; m++)
-                if (m < nmat) x = __fmaf_rn(ad[m], __ldg(p.mu + bin * nmat + m), x);
-            const float e = expf(-x) * __ldg(p.pdf + bin);
-            const float d = -(gI * __ldg(p.energies + bin) + gP) * e;  // dL/dx_bin
+                for (int m = 0; m < M; m++)
+                    if (m < nmat) x = __fmaf_rn(ad[m], __ldg(p.mu + bin * nmat + m), x);
+                const float e = expf(-x) * __ldg(p.pdf + bin);
+                const float d = -(gI * __ldg(p.energies + bin) + gP) * e;  // dL/dx_bin
 #pragma unroll
-            for (int m = 0; m < M; m++)
-                if (m < nmat) gr[m] = __fmaf_rn(d, __ldg(p.mu + bin * nmat + m), gr[m]);
+                for (int m = 0; m < M; m++)
+                    if (m < nmat) gr[m] = __fmaf_rn(d, __ldg(p.mu + bin * nmat + m), gr[m]);
+            }
         }
         const float scale = step / 10.0f;  // AD = raw * step / 10
+        bool any = false;
 #pragma unroll
-        for (int m = 0; m < M; m++) gr[m] *= scale;
+        for (int m = 0; m < M; m++) {
+            gr[m] *= scale;
+            any |= gr[m] != 0.0f;
+        }
 
         // ray setup and live step range: identical to render_ray
         const float uf = (float)u + 0.5f, vf = (float)v + 0.5f;
@@ -136,7 +167,7 @@ __global__ void __launch_bounds__(kBlockThreads) adjoint_kernel(const __grid_con
         const float rzi = dot3(A[6], rx, A[7], ry, A[8], rz);
         const float r3[3] = {rxi, ryi, rzi};
         float mn = 0.0f, mx = p.max_ray_length > 0.0f ? p.max_ray_length : __int_as_float(0x7f800000);
-        bool ok = V.enabled != 0;
+        bool ok = V.enabled != 0 && any;
 #pragma unroll
         for (int ax = 0; ax < 3; ax++) {
             const float s = view.vol[0].s[ax];
@@ -162,20 +193,27 @@ __global__ void __launch_bounds__(kBlockThreads) adjoint_kernel(const __grid_con
             const int t_end = t + advance_alpha(&a_end, step, mx, num_steps - t, true);
             const float sx = view.vol[0].s[0], sy = view.vol[0].s[1], sz = view.vol[0].s[2];
             const int n0 = V.n[0], n1 = V.n[1], n2 = V.n[2];
+            const bool want_density = P.grad_density != nullptr;
             // density-gradient run: texel cell of the hardware filter and its eight contributions
             int ci = -1, cj = -1, ck = -1, ci1 = 0, cj1 = 0, ck1 = 0;
             float acc[8];
 #pragma unroll
             for (int c = 0; c < 8; c++) acc[c] = 0.0f;
-            float Hw[3] = {0.f, 0.f, 0.f}, K[3] = {0.f, 0.f, 0.f};
             auto flush = [&]() {
-                if (ci < 0 || P.grad_density == nullptr) return;
+                if (ci < 0) return;
                 const int is[2] = {ci, ci1}, js[2] = {cj, cj1}, ks[2] = {ck, ck1};
 #pragma unroll
                 for (int c = 0; c < 8; c++)
                     if (acc[c] != 0.0f)
                         atomicAdd(P.grad_density + ((size_t)ks[c >> 2] * n1 + js[(c >> 1) & 1]) * n0 + is[c & 1], acc[c]);
             };
+            // cache of the label cell floor(p): its word, per-corner material weights and texels
+            float pb0 = __int_as_float(0x7fc00000), pb1 = pb0, pb2 = pb0;
+            bool uni = false;
+            float gu = 0.0f, g8[8], rho8[8];
+#pragma unroll
+            for (int c = 0; c < 8; c++) g8[c] = rho8[c] = 0.0f;
+            float Hw[3] = {0.f, 0.f, 0.f}, K[3] = {0.f, 0.f, 0.f};
             for (; t < t_end; ++t) {
                 const float wt = (0 == t || num_steps - 1 == t) ? 0.5f : 1.0f;
                 const float px = __fsub_rn(__fmaf_rn(alpha, rxi, sx), 1.0f);
@@ -183,78 +221,81 @@ __global__ void __launch_bounds__(kBlockThreads) adjoint_kernel(const __grid_con
                 const float pz = __fsub_rn(__fmaf_rn(alpha, rzi, sz), 1.0f);
                 const float bx = floorf(px), by = floorf(py), bz = floorf(pz);
                 const float fx = __fsub_rn(px, bx), fy = __fsub_rn(py, by), fz = __fsub_rn(pz, bz);
-                const uint32_t word = fetch_label_word(V, bx, by, bz);
-                // per-corner material weight and the exact label fractions' projection q = sum_m gr_m seg_m
-                float g8[8];
+                if (bx != pb0 || by != pb1 || bz != pb2) {
+                    const uint32_t word = fetch_label_word(V, bx, by, bz);
+                    uni = uniform_word(word);
+                    gu = gr_of<M>(gr, (int)(word & 15u));
 #pragma unroll
-                for (int c = 0; c < 8; c++) {
-                    const int L = (int)((word >> (4 * c)) & 15u);
-                    float gv = 0.0f;
+                    for (int c = 0; c < 8; c++) g8[c] = uni ? gu : gr_of<M>(gr, (int)((word >> (4 * c)) & 15u));
+                    if (POSE) {
 #pragma unroll
-                    for (int m = 0; m < M; m++)
-                        if (m == L) gv = gr[m];
-                    g8[c] = gv;
-                }
-                const CornerWeights cw = corner_weights(fx, fy, fz);
-                float q = 0.0f;
-#pragma unroll
-                for (int c = 0; c < 8; c++) q = __fmaf_rn(__fmul_rn(cw.xy[c & 3], cw.z[c >> 2]), g8[c], q);
-                // density gradient with the texture unit's corner weights at x = p + 0.5
-                const float tx = __fadd_rn(px, 0.5f), ty = __fadd_rn(py, 0.5f), tz = __fadd_rn(pz, 0.5f);
-                int i0, i1, ax_, j0, j1, ay_, k0, k1, az_;
-                hw_axis(tx, n0, i0, i1, ax_);
-                hw_axis(ty, n1, j0, j1, ay_);
-                hw_axis(tz, n2, k0, k1, az_);
-                if (i0 != ci || j0 != cj || k0 != ck) {
-                    flush();
-                    ci = i0, cj = j0, ck = k0, ci1 = i1, cj1 = j1, ck1 = k1;
-#pragma unroll
-                    for (int c = 0; c < 8; c++) acc[c] = 0.0f;
-                }
-                int W[8];
-                hw_weights(ax_, ay_, az_, W);
-                const float wq = wt * q * (1.0f / 256.0f);
-#pragma unroll
-                for (int c = 0; c < 8; c++) acc[c] = __fmaf_rn(wq, (float)W[c], acc[c]);
-                if (P.grad_pose != nullptr) {
-                    // continuous trilinear of the density texels and of g8 around p (cell floor(p))
-                    float rho8[8];
-#pragma unroll
-                    for (int c = 0; c < 8; c++)
-                        rho8[c] = tex3D<float>(P.density_point, bx + (float)(c & 1) + 0.5f,
-                                               by + (float)((c >> 1) & 1) + 0.5f, bz + (float)(c >> 2) + 0.5f);
-                    const float gx_ = 1.0f - fx, gy_ = 1.0f - fy, gz_ = 1.0f - fz;
-                    const float wxs[2] = {gx_, fx}, wys[2] = {gy_, fy}, wzs[2] = {gz_, fz};
-                    float rho = 0.f, Q = 0.f, drho[3] = {0.f, 0.f, 0.f}, dQ[3] = {0.f, 0.f, 0.f};
-#pragma unroll
-                    for (int c = 0; c < 8; c++) {
-                        const float wx = wxs[c & 1], wy = wys[(c >> 1) & 1], wz = wzs[c >> 2];
-                        const float sxg = (c & 1) ? 1.f : -1.f, syg = ((c >> 1) & 1) ? 1.f : -1.f, szg = (c >> 2) ? 1.f : -1.f;
-                        const float w = wx * wy * wz;
-                        rho += w * rho8[c];
-                        Q += w * g8[c];
-                        const float d0 = sxg * wy * wz, d1 = wx * syg * wz, d2 = wx * wy * szg;
-                        drho[0] += d0 * rho8[c];
-                        drho[1] += d1 * rho8[c];
-                        drho[2] += d2 * rho8[c];
-                        dQ[0] += d0 * g8[c];
-                        dQ[1] += d1 * g8[c];
-                        dQ[2] += d2 * g8[c];
+                        for (int c = 0; c < 8; c++)
+                            rho8[c] = tex3D<float>(P.density_point, bx + (float)(c & 1) + 0.5f,
+                                                   by + (float)((c >> 1) & 1) + 0.5f, bz + (float)(c >> 2) + 0.5f);
                     }
-                    const float h[3] = {wt * (drho[0] * Q + rho * dQ[0]), wt * (drho[1] * Q + rho * dQ[1]),
-                                        wt * (drho[2] * Q + rho * dQ[2])};
+                    pb0 = bx;
+                    pb1 = by;
+                    pb2 = bz;
+                }
+                const float gx = 1.0f - fx, gy = 1.0f - fy, gz = 1.0f - fz;
+                // q = sum_m gr_m seg_m: the derivative of this sample's contribution by its density
+                float q = gu;
+                if (!uni) {
+                    const CornerWeights cw = corner_weights(fx, fy, fz);
+                    q = 0.0f;
+#pragma unroll
+                    for (int c = 0; c < 8; c++) q = __fmaf_rn(__fmul_rn(cw.xy[c & 3], cw.z[c >> 2]), g8[c], q);
+                }
+                if (want_density) {
+                    // density gradient with the texture unit's corner weights at x = p + 0.5
+                    int i0, i1, ax_, j0, j1, ay_, k0, k1, az_;
+                    hw_axis(__fadd_rn(px, 0.5f), n0, i0, i1, ax_);
+                    hw_axis(__fadd_rn(py, 0.5f), n1, j0, j1, ay_);
+                    hw_axis(__fadd_rn(pz, 0.5f), n2, k0, k1, az_);
+                    if (i0 != ci || j0 != cj || k0 != ck) {
+                        flush();
+                        ci = i0, cj = j0, ck = k0, ci1 = i1, cj1 = j1, ck1 = k1;
+#pragma unroll
+                        for (int c = 0; c < 8; c++) acc[c] = 0.0f;
+                    }
+                    int W[8];
+                    hw_weights(ax_, ay_, az_, W);
+                    const float wq = wt * q * (1.0f / 256.0f);
+#pragma unroll
+                    for (int c = 0; c < 8; c++) acc[c] = __fmaf_rn(wq, (float)W[c], acc[c]);
+                }
+                if (POSE) {
+                    // h = d/dp of w_t rho(p) Q(p), rho and Q the continuous trilinear interpolants of
+                    // the cell's texels and per-corner material weights
+                    float dr[3];
+                    trilinear_grad(rho8, fx, fy, fz, gx, gy, gz, dr);
+                    float h[3];
+                    if (uni) {
+                        const float wQ = wt * gu;
+                        h[0] = wQ * dr[0];
+                        h[1] = wQ * dr[1];
+                        h[2] = wQ * dr[2];
+                    } else {
+                        float dQ[3];
+                        trilinear_grad(g8, fx, fy, fz, gx, gy, gz, dQ);
+                        const float rho = trilinear(rho8, fx, fy, fz, gx, gy, gz);
+                        const float Q = trilinear(g8, fx, fy, fz, gx, gy, gz);
+                        h[0] = wt * (dr[0] * Q + rho * dQ[0]);
+                        h[1] = wt * (dr[1] * Q + rho * dQ[1]);
+                        h[2] = wt * (dr[2] * Q + rho * dQ[2]);
+                    }
                     // q_w = A^T h (world-space derivative), accumulated plain and weighted by alpha
 #pragma unroll
                     for (int k = 0; k < 3; k++) {
                         const float qw = A[k] * h[0] + A[3 + k] * h[1] + A[6 + k] * h[2];
                         Hw[k] += qw;
-                        K[k] += alpha * qw;
+                        K[k] = __fmaf_rn(alpha, qw, K[k]);
                     }
                 }
                 alpha = __fadd_rn(alpha, step);
             }
-            flush();
-            if (P.grad_pose != nullptr) {
+            if (want_density) flush();
+            if (POSE) {
                 const float d[3] = {av.source_world[0] - P.center[0], av.source_world[1] - P.center[1],
                                     av.source_world[2] - P.center[2]};
                 const float r[3] = {rx, ry, rz};
@@ -267,7 +308,7 @@ __global__ void __launch_bounds__(kBlockThreads) adjoint_kernel(const __grid_con
             }
         }
     }
-    if (P.grad_pose != nullptr && zv < P.n_views) {
+    if (POSE && zv < P.n_views) {
         // one view per block: reduce over the warp, then one atomic per warp and component
 #pragma unroll
         for (int k = 0; k < 6; k++) {

@@ -245,7 +245,13 @@ static void attenuate_f32(const orc_scene *sc, const float *ad, float *I, float 
 /* One ray in the reference's float32 arithmetic. ad_out receives the per-material area densities
  * in g/cm^2 (project_kernel.cu:558-584). Returns the number of samples (t, volume) with the volume
  * traced, enabled and alpha inside its interval. */
-static double ray_f32(const orc_scene *sc, int u, int v, float *ad_out, float *I, float *P) {
+/* Optional record of the samples of one single-volume ray (orc_ray_samples_f32). */
+typedef struct {
+    float *alpha, *p, *w;
+    int cap, n;
+} orc_rec;
+
+static double ray_f32(const orc_scene *sc, int u, int v, float *ad_out, float *I, float *P, orc_rec *rec) {
     const int NV = sc->n_volumes, M = sc->n_materials;
     const float *W = sc->world_from_index;
     const float step = sc->step;
@@ -389,6 +395,14 @@ static double ray_f32(const orc_scene *sc, int u, int v, float *ad_out, float *I
                     float rho = (float)(V->half_filter ? round_to_half(rho_d) : rho_d);
                     float wr = weight * rho;
                     for (int m = 0; m < M; m++) ad[m] = fmaf(wr, seg[vol][m], ad[m]);
+                    if (rec && rec->n < rec->cap) {
+                        rec->alpha[rec->n] = alpha;
+                        rec->p[3 * rec->n] = px[vol];
+                        rec->p[3 * rec->n + 1] = py[vol];
+                        rec->p[3 * rec->n + 2] = pz[vol];
+                        rec->w[rec->n] = weight;
+                        rec->n++;
+                    }
                 }
             }
         }
@@ -564,7 +578,7 @@ int orc_project(const orc_scene *sc, int mode, const int64_t *ray_ids, int64_t n
         int u = (int)(pix % sc->width), v = (int)(pix / sc->width);
         if (mode == ORC_MODE_F32) {
             float ad[ORC_MAX_MAT], I, P;
-            nsamp += ray_f32(sc, u, v, ad, &I, &P);
+            nsamp += ray_f32(sc, u, v, ad, &I, &P, NULL);
             ((float *)intensity)[r] = I;
             ((float *)photon_prob)[r] = P;
             if (area_density)
@@ -580,6 +594,18 @@ int orc_project(const orc_scene *sc, int mode, const int64_t *ray_ids, int64_t n
     }
     if (samples) *samples = nsamp;
     return 0;
+}
+
+/* The samples ORC_MODE_F32 takes along ray (u, v) of a single-volume scene: per contributing step
+ * its float32 alpha, position p = (x, y, z) in the volume's shifted IJK frame (the -1 voxel offset
+ * applied) and trapezoid weight, in march order. Returns how many were taken (at most `cap` are
+ * written), or -1 for a scene with other than one volume. */
+int orc_ray_samples_f32(const orc_scene *sc, int u, int v, float *alpha, float *p, float *w, int cap) {
+    if (!sc || sc->n_volumes != 1) return -1;
+    orc_rec rec = {alpha, p, w, cap, 0};
+    float ad[ORC_MAX_MAT], I, P;
+    double n = ray_f32(sc, u, v, ad, &I, &P, &rec);
+    return n > (double)cap ? (int)n : rec.n;
 }
 
 /* Texture-filter emulation exposed for the tests that pin it against the GPU's texture unit. */

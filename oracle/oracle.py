@@ -86,6 +86,9 @@ def lib() -> ctypes.CDLL:
                                      ctypes.POINTER(ctypes.c_double), ctypes.c_int]
         _lib.orc_tex_linear.restype = ctypes.c_double
         _lib.orc_tex_linear.argtypes = [ctypes.POINTER(_Scene), ctypes.c_int] + [ctypes.c_double] * 3
+        _lib.orc_ray_samples_f32.restype = ctypes.c_int
+        _lib.orc_ray_samples_f32.argtypes = [ctypes.POINTER(_Scene), ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                             ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
         _lib.orc_tex_point.restype = ctypes.c_int
         _lib.orc_tex_point.argtypes = [ctypes.POINTER(_Scene), ctypes.c_int] + [ctypes.c_double] * 3
     return _lib
@@ -195,6 +198,18 @@ class Scene:
         else:
             ad = ad.reshape(M, n)
         return dict(intensity=inten, photon_prob=prob, area_density=ad, samples=samples.value)
+
+    def ray_samples(self, u: int, v: int, cap: int = 1 << 20):
+        """The float32-mode samples of ray (u, v) of a one-volume scene: (alpha [n], p [n, 3], weight [n]),
+        float32, p in the shifted IJK frame of the march."""
+        alpha = np.empty(cap, dtype=np.float32)
+        p = np.empty((cap, 3), dtype=np.float32)
+        w = np.empty(cap, dtype=np.float32)
+        n = lib().orc_ray_samples_f32(ctypes.byref(self.sc), int(u), int(v), alpha.ctypes.data, p.ctypes.data,
+                                      w.ctypes.data, cap)
+        if n < 0 or n > cap:
+            raise ValueError("ray_samples needs a one-volume scene and room for every sample")
+        return alpha[:n], p[:n], w[:n]
 
     def tex_linear(self, vol: int, x: float, y: float, z: float) -> float:
         return lib().orc_tex_linear(ctypes.byref(self.sc), vol, x, y, z)

@@ -5,10 +5,11 @@ Tolerances (stated per test):
     relative to sum |c * A rho| (float32 forward and float32 atomics);
   * spectral chain: the adjoint fed dL/d(intensity), dL/d(photon_prob) equals the adjoint fed the
     float64 torch-autograd dL/d(area density) of the same Beer-Lambert sum, 1e-5 of max |grad|;
-  * central finite differences (h = 1e-3) of the float64 oracle (exact trilinear filter, float64
-    positions) against the gradients: 1e-2 relative for densities (the product's gradient is that
-    of the texture unit's 8-bit weights), 2e-2 of the largest component for the pose (surrogate
-    derivative, entry and exit samples held fixed).
+  * float64 autograd of the restatement in tests/fp64_reference.py, evaluated at the product's own
+    float32 sample positions: density gradients per voxel within 1e-4 of the largest, pose
+    gradients within 2e-3 of the largest component;
+  * central finite differences (h = 1e-3): of that restatement for densities (1e-4), of the
+    float64 oracle for the pose (see test_pose_gradient_... for the rotation tolerance).
 """
 import numpy as np
 import pytest
@@ -24,6 +25,7 @@ from deepdrr_gb300.phantoms import random_views
 from deepdrr_gb300.volume import Volume
 from oracle import oracle
 
+from fp64_reference import project_fp64_at_samples
 from helpers import GOLDEN_TABLES, labels_for, material_list
 
 pytestmark = pytest.mark.gpu
@@ -124,43 +126,79 @@ def test_spectral_chain_matches_float64_autograd():
         assert err <= 1e-5
 
 
-def test_density_gradient_matches_float64_finite_differences():
+def scene_tables(vol):
+    src = tables.NpzTables(GOLDEN_TABLES)
+    mats = material_list([vol])
+    e, pdf, mu = tables.build_tables("90KV_AL40", mats, src)
+    return e, pdf, mu, labels_for(vol, mats)
+
+
+def reference_loss(vol, projs, ijk_at, a, b, density, pose=None, center=None, filter="exact"):
+    """sum_views sum(a I + b P) of the float64 autograd restatement at the product's own float32
+    sample positions (taken with IJK_from_world = ijk_at, recorded by the float32 oracle)."""
+    e, pdf, mu, labels = scene_tables(vol)
+    L = 0.0
+    for k, proj in enumerate(projs):
+        W, s, w, h = geo.view_arrays(proj)
+        sc = oracle.Scene([dict(density=vol.data, labels=labels, ijk_from_world=ijk_at)], W, s, width=w, height=h,
+                          step=STEP, energies=e, pdf=pdf, mu=mu, max_ray_length=-1.0)
+        samples = [sc.ray_samples(u, v) for v in range(h) for u in range(w)]
+        I, P, _ = project_fp64_at_samples(density, labels, ijk_at, samples, w, h, STEP, e, pdf, mu, pose=pose,
+                                          ijk0=np.asarray(vol.ijk_from_world.data), center=center, filter=filter)
+        L = L + (torch.from_numpy(a[k]) * I).sum() + (torch.from_numpy(b[k]) * P).sum()
+    return L
+
+
+def test_density_gradient_matches_float64_autograd_and_finite_differences():
     vol, projs = scene()
     rng = np.random.default_rng(3)
+    n = len(projs)
+    H, W = projs[0].intrinsic.sensor_height, projs[0].intrinsic.sensor_width
+    a = rng.standard_normal((n, H, W))
+    b = rng.standard_normal((n, H, W))
     with projector(vol) as p:
-        n = len(projs)
-        H, W = projs[0].intrinsic.sensor_height, projs[0].intrinsic.sensor_width
-        a = rng.standard_normal((n, H, W))
-        b = rng.standard_normal((n, H, W))
-        rho0 = vol.data.astype(np.float32)
-        rho = torch.from_numpy(rho0).cuda().requires_grad_()
+        rho = torch.from_numpy(vol.data.astype(np.float32)).cuda().requires_grad_()
         out = project_ad(p, *projs, density=rho)
         L = (torch.from_numpy(a).cuda() * out["intensity"].double()).sum() + \
             (torch.from_numpy(b).cuda() * out["photon_prob"].double()).sum()
         L.backward()
-        grad = rho.grad.double().cpu().numpy()
-        ijk4 = np.asarray(vol.ijk_from_world.data)
-        interior = vol.data > 0
-        for trial in range(2):
-            delta = rng.standard_normal(vol.shape) * interior
-            h = 1e-3
-            lp = oracle_loss(vol, (rho0 + h * delta).astype(np.float64), ijk4, projs, a, b)
-            lm = oracle_loss(vol, (rho0 - h * delta).astype(np.float64), ijk4, projs, a, b)
-            fd = (lp - lm) / (2 * h)
-            an = float((grad * delta).sum())
-            print(f"density FD trial {trial}: fd {fd:.9g} adjoint {an:.9g} rel {abs(fd - an) / abs(fd):.2e}")
-            assert abs(fd - an) <= 1e-2 * abs(fd)
+        g = rho.grad.double().cpu()
+    ijk0 = np.asarray(vol.ijk_from_world.data)
+    d64 = torch.from_numpy(vol.data.astype(np.float64)).requires_grad_()
+    reference_loss(vol, projs, ijk0, a, b, d64, filter="hw").backward()
+    g_ref = d64.grad
+    err = float((g - g_ref).abs().max() / g_ref.abs().max())
+    print(f"density gradient vs float64 autograd: max |diff| / max |ref| = {err:.2e}")
+    assert err <= 1e-4
+    # central differences of the float64 restatement (linear in the densities along a direction)
+    delta = torch.from_numpy(rng.standard_normal(vol.shape) * (vol.data > 0))
+    h = 1e-3
+    with torch.no_grad():
+        base = torch.from_numpy(vol.data.astype(np.float64))
+        lp = reference_loss(vol, projs, ijk0, a, b, base + h * delta, filter="hw")
+        lm = reference_loss(vol, projs, ijk0, a, b, base - h * delta, filter="hw")
+    fd = float((lp - lm) / (2 * h))
+    an = float((g * delta).sum())
+    print(f"density FD (h=1e-3) {fd:.9g} vs adjoint {an:.9g}: rel {abs(fd - an) / abs(fd):.2e}")
+    assert abs(fd - an) <= 1e-4 * abs(fd)
 
 
 @pytest.mark.parametrize("pose0", [np.zeros(6), np.array([0.4, -0.3, 0.2, 0.03, -0.02, 0.04])])
-def test_pose_gradient_matches_float64_finite_differences(pose0):
+def test_pose_gradient_matches_float64_autograd_and_finite_differences(pose0):
+    """Against the float64 autograd restatement at the product's own sample positions: 2e-3 of
+    the largest component (the product's material weights come from the texture unit's 8-bit
+    density filter, the restatement's from the exact one). Central differences (h = 1e-3) of the
+    float64 oracle: translations within 5e-3 and rotations within 6e-2 of the largest component.
+    The interpolant is trilinear, so its derivative jumps at voxel faces; a 1e-3 rad turn moves
+    samples near the volume's rim by ~0.01 voxel and the central difference then mixes the slopes
+    of neighbouring cells (it converges to the derivative as h shrinks)."""
     vol, projs = scene()
     rng = np.random.default_rng(4)
+    n = len(projs)
+    H, W = projs[0].intrinsic.sensor_height, projs[0].intrinsic.sensor_width
+    a = rng.standard_normal((n, H, W))
+    b = rng.standard_normal((n, H, W))
     with projector(vol) as p:
-        n = len(projs)
-        H, W = projs[0].intrinsic.sensor_height, projs[0].intrinsic.sensor_width
-        a = rng.standard_normal((n, H, W))
-        b = rng.standard_normal((n, H, W))
         center = p.volume_center_world(0)
         pose = torch.tensor(pose0, dtype=torch.float64, requires_grad=True)
         out = project_ad(p, *projs, pose=pose, center=center)
@@ -168,18 +206,26 @@ def test_pose_gradient_matches_float64_finite_differences(pose0):
             (torch.from_numpy(b).cuda() * out["photon_prob"].double()).sum()
         L.backward()
         g = pose.grad.numpy()
-        ijk0 = np.asarray(vol.ijk_from_world.data)
-        dens = vol.data.astype(np.float64)
-        fd = np.zeros(6)
-        h = 1e-3
-        for k in range(6):
-            e = np.zeros(6)
-            e[k] = h
-            lp = oracle_loss(vol, dens, ijk0 @ np.linalg.inv(rigid_motion(pose0 + e, center)), projs, a, b)
-            lm = oracle_loss(vol, dens, ijk0 @ np.linalg.inv(rigid_motion(pose0 - e, center)), projs, a, b)
-            fd[k] = (lp - lm) / (2 * h)
-        print(f"pose gradient at {pose0}:\n  adjoint {g}\n  fd      {fd}")
-        assert np.abs(g - fd).max() <= 2e-2 * np.abs(fd).max()
+    ijk0 = np.asarray(vol.ijk_from_world.data)
+    ijk_at = ijk0 @ np.linalg.inv(rigid_motion(pose0, center))
+    pr = torch.tensor(pose0, dtype=torch.float64, requires_grad=True)
+    reference_loss(vol, projs, ijk_at, a, b, torch.from_numpy(vol.data.astype(np.float64)), pose=pr,
+                   center=center).backward()
+    g_ref = pr.grad.numpy()
+    dens = vol.data.astype(np.float64)
+    fd = np.zeros(6)
+    h = 1e-3
+    for k in range(6):
+        e = np.zeros(6)
+        e[k] = h
+        lp = oracle_loss(vol, dens, ijk0 @ np.linalg.inv(rigid_motion(pose0 + e, center)), projs, a, b)
+        lm = oracle_loss(vol, dens, ijk0 @ np.linalg.inv(rigid_motion(pose0 - e, center)), projs, a, b)
+        fd[k] = (lp - lm) / (2 * h)
+    print(f"pose gradient at {pose0}:\n  adjoint  {g}\n  autograd {g_ref}\n  fd       {fd}")
+    scale = np.abs(g_ref).max()
+    assert np.abs(g - g_ref).max() <= 2e-3 * scale
+    assert np.abs(g[:3] - fd[:3]).max() <= 5e-3 * scale
+    assert np.abs(g[3:] - fd[3:]).max() <= 6e-2 * scale
 
 
 def test_recompute_matches_stored_area_densities():
