@@ -6,6 +6,7 @@ polychromatic Beer-Lambert attenuation with optional neglog, all in hand-written
 reached through the C ABI of ``libdrr_gb300.so`` (``include/drr_gb300.h``).
 """
 from . import geo, tables
+from .device import CameraProjectionDevice, Device, MobileCArm, SimpleDevice
 from .geo import CameraIntrinsicTransform, CameraProjection, FrameTransform
 from .projector import DeprecationError, Projector
 from .volume import Volume, format_materials, hu_to_density, segment_thresholds
@@ -14,5 +15,5 @@ __version__ = "0.1.0"
 
 __all__ = [
     "Projector", "Volume", "CameraIntrinsicTransform", "CameraProjection", "FrameTransform",
-    "DeprecationError", "geo", "tables", "hu_to_density", "segment_thresholds", "format_materials",
+    "DeprecationError", "geo", "tables", "Device", "SimpleDevice", "MobileCArm", "CameraProjectionDevice", "hu_to_density", "segment_thresholds", "format_materials",
 ]

@@ -269,6 +269,11 @@ class Projector:
     def _prepare_project(self, camera_projections):
         if not self.initialized:
             raise RuntimeError("Projector has not been initialized.")
+        return self._views(camera_projections)
+
+    def _views(self, camera_projections):
+        """The camera projections of a call (the device's current view when none are given) and
+        the maximum ray length that goes with them (projector.py:641-650)."""
         if not camera_projections and self.device is None:
             raise ValueError("must provide a camera projection object to the projector, unless imaging device "
                              "(e.g. CArm) is provided")
