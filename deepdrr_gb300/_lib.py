@@ -21,6 +21,10 @@ DRR_DENSITY_F32 = 0
 DRR_DENSITY_F16 = 1
 DRR_DENSITY_BF16 = 2
 
+DRR_HU_F32 = 0
+DRR_HU_I16 = 1
+DRR_HU_F64 = 2
+
 DRR_MAX_VOLUMES = 4
 DRR_MAX_MATERIALS = 16
 
@@ -30,7 +34,7 @@ DRR_FLAG_PERSISTENT = 1 << 2
 
 # Every symbol the header declares; the CPU test suite checks that the library exports all of them.
 EXPORTED_SYMBOLS = (
-    "drr_volset_create", "drr_volset_destroy", "drr_volset_set_density", "drr_tables_create", "drr_tables_destroy",
+    "drr_volset_create", "drr_volset_destroy", "drr_volset_set_density", "drr_ingest_hu", "drr_tables_create", "drr_tables_destroy",
     "drr_project", "drr_project_adjoint", "drr_graph_create", "drr_graph_set_views", "drr_graph_launch", "drr_graph_destroy",
     "drr_autotune", "drr_add_noise", "drr_poisson_sample", "drr_neglog", "drr_neglog_noalloc", "drr_clip_upper", "drr_last_error", "drr_version",
 )
@@ -109,6 +113,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     lib.drr_volset_destroy.restype = st
     lib.drr_volset_set_density.argtypes = [vp, i32, vp, vp]
     lib.drr_volset_set_density.restype = st
+    lib.drr_ingest_hu.argtypes = [vp, i32, i32, i32, i32, ctypes.POINTER(ctypes.c_uint8), vp, i32, vp, vp]
+    lib.drr_ingest_hu.restype = st
     lib.drr_tables_create.argtypes = [vp, vp, vp, i32, i32, vp, ctypes.POINTER(vp)]
     lib.drr_tables_create.restype = st
     lib.drr_tables_destroy.argtypes = [vp]

@@ -198,9 +198,13 @@ class Projector:
                       "bfloat16": _lib.DRR_DENSITY_BF16}[self.density_dtype]
         with torch.cuda.device(self.torch_device):
             for i, v in enumerate(self.volumes):
+                ingested = v.device_arrays(self.torch_device) if hasattr(v, "device_arrays") else None
                 # reference layout [i, j, k] -> texture layout [k][j][i] (projector.py:1469)
-                dens = torch.from_numpy(np.ascontiguousarray(v.data, dtype=np.float32)).to(self.torch_device)
-                dens = dens.permute(2, 1, 0).contiguous()
+                if ingested is not None:
+                    dens = ingested[0]
+                else:
+                    dens = torch.from_numpy(np.ascontiguousarray(v.data, dtype=np.float32)).to(self.torch_device)
+                    dens = dens.permute(2, 1, 0).contiguous()
                 if self.density_dtype == "float16":
                     dens = dens.half()
                 elif self.density_dtype == "bfloat16":
@@ -211,9 +215,12 @@ class Projector:
                 for name, idx in names.items():
                     if name in self.all_materials:
                         lut[idx] = self.all_materials.index(name)
-                seg_t = torch.from_numpy(np.ascontiguousarray(seg.astype(np.int64))).to(self.torch_device)
                 lut_t = torch.from_numpy(lut).to(self.torch_device)
-                labels = lut_t[seg_t].permute(2, 1, 0).contiguous()
+                if ingested is not None:
+                    labels = lut_t[ingested[1].long()]
+                else:
+                    seg_t = torch.from_numpy(np.ascontiguousarray(seg.astype(np.int64))).to(self.torch_device)
+                    labels = lut_t[seg_t].permute(2, 1, 0).contiguous()
                 keep += [dens, labels]
                 d = descs[i]
                 d.density = dens.data_ptr()

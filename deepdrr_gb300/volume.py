@@ -104,15 +104,47 @@ class Volume:
     @classmethod
     def from_hu(cls, hu_values: np.ndarray, origin=(0.0, 0.0, 0.0), use_thresholding: bool = True,
                 spacing=(1.0, 1.0, 1.0), anatomical_coordinate_system: Optional[str] = None,
-                world_from_anatomical: Optional[FrameTransform] = None, **kwargs) -> "Volume":
-        """HU -> density and threshold segmentation (volume.py:281-302)."""
+                world_from_anatomical: Optional[FrameTransform] = None, device=None, **kwargs) -> "Volume":
+        """HU -> density and threshold segmentation (volume.py:281-302).
+
+        With ``device`` (a CUDA device, or ``hu_values`` given as a CUDA tensor) the conversion runs
+        on the GPU (drr_ingest_hu, same results bit for bit); the volume keeps the device arrays in
+        the projector's layout and ``Projector.initialize`` uses them instead of uploading ``data``
+        again, as long as ``data`` and the label array are the arrays made here."""
         if not use_thresholding:
             raise NotImplementedError("network segmentation is outside the projection path")
-        data = hu_to_density(hu_values).astype(np.float32)
-        materials = segment_thresholds(hu_values)
-        return cls.from_parameters(data, materials, origin=origin, spacing=spacing,
-                                   anatomical_coordinate_system=anatomical_coordinate_system,
-                                   world_from_anatomical=world_from_anatomical, **kwargs)
+        on_gpu = device is not None or type(hu_values).__module__.startswith("torch")
+        if not on_gpu:
+            data = hu_to_density(hu_values).astype(np.float32)
+            materials = segment_thresholds(hu_values)
+            return cls.from_parameters(data, materials, origin=origin, spacing=spacing,
+                                       anatomical_coordinate_system=anatomical_coordinate_system,
+                                       world_from_anatomical=world_from_anatomical, **kwargs)
+        import torch
+
+        from .ingest import hu_to_density_and_labels
+
+        hu = hu_values if isinstance(hu_values, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(hu_values))
+        hu = hu.to(torch.device(device) if device is not None else hu.device)
+        density, labels = hu_to_density_and_labels(hu)
+        data = density.permute(2, 1, 0).cpu().numpy()
+        ids = labels.permute(2, 1, 0).cpu().numpy().astype(np.uint16)
+        names = {"air": 0, "soft tissue": 1, "bone": 2}
+        vol = cls.from_parameters(data, (names, ids), origin=origin, spacing=spacing,
+                                  anatomical_coordinate_system=anatomical_coordinate_system,
+                                  world_from_anatomical=world_from_anatomical, **kwargs)
+        vol._device_arrays = dict(density=density, labels=labels, data=vol.data, ids=vol.materials[1])
+        return vol
+
+    def device_arrays(self, device):
+        """(density [nk, nj, ni] float32, material ids [nk, nj, ni] uint8) on ``device`` if this volume
+        was ingested on the GPU and its arrays are unchanged, else None."""
+        d = getattr(self, "_device_arrays", None)
+        if d is None or d["data"] is not self.data or d["ids"] is not self.materials[1]:
+            return None
+        if d["density"].device != device:
+            return None
+        return d["density"], d["labels"]
 
     # ---- pose --------------------------------------------------------------------------------
     @property

@@ -15,6 +15,7 @@
  *   drr_project         Projector._render_single + _update_object_locations + the projectKernel
  *                       launch, projector.py:709-800, 802-831; kernel deepdrr/projector/project_kernel.cu:135-650
  *   drr_*_destroy       Projector.free, projector.py:1719-1764
+ *   drr_ingest_hu       Volume.from_hu's HU conversion and thresholding, deepdrr/vol/volume.py:281-351
  *   drr_add_noise       analytic_generators.add_noise, deepdrr/projector/analytic_generators.py:10-18
  *   drr_clip_upper,     the post-processing of Projector.project, projector.py:697-702, and
  *   drr_neglog          deepdrr/utils/image_utils.py:18-58
@@ -81,6 +82,23 @@ drr_status drr_volset_destroy(drr_volset *set);
  * bfloat16 volume returns DRR_ERR_UNSUPPORTED). Labels are kept. No counterpart in the reference:
  * it lets a differentiable caller project the current iterate without rebuilding the set. */
 drr_status drr_volset_set_density(drr_volset *set, int32_t volume, const void *density, void *stream);
+
+typedef enum {
+    DRR_HU_F32 = 0, /* float32 Hounsfield units (converted in float32, as numpy does) */
+    DRR_HU_I16 = 1, /* int16 Hounsfield units (converted in float64, then rounded to float32) */
+    DRR_HU_F64 = 2  /* float64 Hounsfield units (likewise) */
+} drr_hu_type;
+
+/* Volume ingest on the GPU: replaces the numpy work of Volume.from_hu (deepdrr/vol/volume.py:281-302:
+ * _convert_hounsfield_to_density, volume.py:339-351, and the thresholding of load_dicom.py:132-143)
+ * and the i-fastest layout change of projector.py:1469. `hu` is a DEVICE array [ni][nj][nk] (k
+ * fastest, the reference's layout); `density` (drr_density_type, float32 / float16 / bfloat16 rounded
+ * to nearest) and `labels` are DEVICE arrays [nk][nj][ni] ready for drr_volume_desc. class_labels
+ * (host) are the labels written for air (HU <= -800), soft tissue (-800 < HU <= 350) and bone
+ * (HU > 350); NaN HU are air. Asynchronous on `stream`. */
+drr_status drr_ingest_hu(const void *hu, int32_t hu_type, int32_t ni, int32_t nj, int32_t nk,
+                         const uint8_t class_labels[3], void *density, int32_t density_type, uint8_t *labels,
+                         void *stream);
 
 /* Upload a spectrum and its mass-attenuation table. Host pointers:
  *   energies_kev [n_bins], pdf [n_bins], mu_over_rho [n_bins][n_materials] (cm^2/g).
