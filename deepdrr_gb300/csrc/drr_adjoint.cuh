@@ -161,7 +161,11 @@ __global__ void __launch_bounds__(kBlockThreads) adjoint_kernel(const __grid_con
         rx = __fmul_rn(rx, inv_norm);
         ry = __fmul_rn(ry, inv_norm);
         rz = __fmul_rn(rz, inv_norm);
-        const float *A = view.vol[0].a;
+        // the view's IJK_from_world rotation in registers: the loop's atomics could alias the view
+        // records as far as the compiler knows, so reads through the pointer would repeat per sample
+        float A[9];
+#pragma unroll
+        for (int k = 0; k < 9; k++) A[k] = view.vol[0].a[k];
         const float rxi = dot3(A[0], rx, A[1], ry, A[2], rz);
         const float ryi = dot3(A[3], rx, A[4], ry, A[5], rz);
         const float rzi = dot3(A[6], rx, A[7], ry, A[8], rz);
@@ -194,6 +198,7 @@ __global__ void __launch_bounds__(kBlockThreads) adjoint_kernel(const __grid_con
             const float sx = view.vol[0].s[0], sy = view.vol[0].s[1], sz = view.vol[0].s[2];
             const int n0 = V.n[0], n1 = V.n[1], n2 = V.n[2];
             const bool want_density = P.grad_density != nullptr;
+            float *const grad_density = P.grad_density;
             // density-gradient run: texel cell of the hardware filter and its eight contributions
             int ci = -1, cj = -1, ck = -1, ci1 = 0, cj1 = 0, ck1 = 0;
             float acc[8];
@@ -205,7 +210,7 @@ __global__ void __launch_bounds__(kBlockThreads) adjoint_kernel(const __grid_con
 #pragma unroll
                 for (int c = 0; c < 8; c++)
                     if (acc[c] != 0.0f)
-                        atomicAdd(P.grad_density + ((size_t)ks[c >> 2] * n1 + js[(c >> 1) & 1]) * n0 + is[c & 1], acc[c]);
+                        atomicAdd(grad_density + ((size_t)ks[c >> 2] * n1 + js[(c >> 1) & 1]) * n0 + is[c & 1], acc[c]);
             };
             // cache of the label cell floor(p): its word, per-corner material weights and texels
             float pb0 = __int_as_float(0x7fc00000), pb1 = pb0, pb2 = pb0;
