@@ -377,20 +377,32 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
         const float rx0 = rxi[0], ry0 = ryi[0], rz0 = rzi[0];
         int cur_m = -1;      // material whose accumulator is held in cur_ad
         float cur_ad = 0.0f;
-        int uni_label = -1;  // label of the cached neighbourhood if its eight labels agree, else -1
+        // Software pipelining of the label words: each step loads the word of the NEXT sample's
+        // base, so the load's latency overlaps this sample's work and no lane branches to fetch.
+        // With one volume the reference's cache always holds the current base's word, so loading
+        // it for every sample is the same thing.
+        float cx = 0.0f, cy = 0.0f, cz = 0.0f, cbx = 0.0f, cby = 0.0f, cbz = 0.0f;
+        uint32_t w_cur = 0;
+        if (t < t_end) {
+            cx = __fsub_rn(__fmaf_rn(alpha, rx0, sx), 1.0f);
+            cy = __fsub_rn(__fmaf_rn(alpha, ry0, sy), 1.0f);
+            cz = __fsub_rn(__fmaf_rn(alpha, rz0, sz), 1.0f);
+            cbx = floorf(cx);
+            cby = floorf(cy);
+            cbz = floorf(cz);
+            w_cur = fetch_label_word(V, cbx, cby, cbz);
+        }
         auto sample = [&](float wscale) {
-            const float px = __fsub_rn(__fmaf_rn(alpha, rx0, sx), 1.0f);
-            const float py = __fsub_rn(__fmaf_rn(alpha, ry0, sy), 1.0f);
-            const float pz = __fsub_rn(__fmaf_rn(alpha, rz0, sz), 1.0f);
-            const float bx = floorf(px), by = floorf(py), bz = floorf(pz);
-            const float fx = __fsub_rn(px, bx), fy = __fsub_rn(py, by), fz = __fsub_rn(pz, bz);
-            if (bx != pb0 || by != pb1 || bz != pb2) {
-                word = fetch_label_word(V, bx, by, bz);
-                uni_label = uniform_word(word) ? (int)(word & 15u) : -1;
-                pb0 = bx;
-                pb1 = by;
-                pb2 = bz;
-            }
+            const float an = __fadd_rn(alpha, step);
+            const float nx = __fsub_rn(__fmaf_rn(an, rx0, sx), 1.0f);
+            const float ny = __fsub_rn(__fmaf_rn(an, ry0, sy), 1.0f);
+            const float nz = __fsub_rn(__fmaf_rn(an, rz0, sz), 1.0f);
+            const float nbx = floorf(nx), nby = floorf(ny), nbz = floorf(nz);
+            const uint32_t w_next = fetch_label_word(V, nbx, nby, nbz);
+            const float px = cx, py = cy, pz = cz;
+            const float fx = __fsub_rn(px, cbx), fy = __fsub_rn(py, cby), fz = __fsub_rn(pz, cbz);
+            word = w_cur;
+            const int uni_label = uniform_word(word) ? (int)(word & 15u) : -1;
             const CornerWeights cw = corner_weights(fx, fy, fz);
             const float rho = tex3D<float>(V.density, __fadd_rn(px, 0.5f), __fadd_rn(py, 0.5f), __fadd_rn(pz, 0.5f));
             const float wr = __fmul_rn(wscale, rho);
@@ -405,12 +417,38 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
             } else {
                 if (cur_m >= 0) store_ad<M>(ad, cur_m, cur_ad);
                 cur_m = -1;
-                float seg[M];
-                label_fractions<M>(word, cw, seg);
+                // two labels A (corner 0's) and B: one pass over the corners into two sums, each
+                // in corner order as the reference accumulates them; other materials get
+                // fma(wr, 0, ad) = ad, exactly what the general path does for them
+                const uint32_t A = word & 15u;
+                const uint32_t xa = word ^ (A * 0x11111111u);
+                const int pos = (__ffs(xa) - 1) & ~3;
+                const uint32_t B = (word >> pos) & 15u;
+                const uint32_t xb = word ^ (B * 0x11111111u);
+                const uint32_t za = ~(((xa & 0x77777777u) + 0x77777777u) | xa) & 0x88888888u;
+                const uint32_t zb = ~(((xb & 0x77777777u) + 0x77777777u) | xb) & 0x88888888u;
+                if ((za | zb) == 0x88888888u) {
+                    float sA = 0.0f, sB = 0.0f;
 #pragma unroll
-                for (int m = 0; m < M; m++) ad[m] = __fmaf_rn(wr, seg[m], ad[m]);
+                    for (int c = 0; c < 8; c++) {
+                        if ((za >> (4 * c + 3)) & 1u)
+                            sA = __fmaf_rn(cw.xy[c & 3], cw.z[c >> 2], sA);
+                        else
+                            sB = __fmaf_rn(cw.xy[c & 3], cw.z[c >> 2], sB);
+                    }
+#pragma unroll
+                    for (int m = 0; m < M; m++)
+                        ad[m] = __fmaf_rn(wr, (uint32_t)m == A ? sA : ((uint32_t)m == B ? sB : 0.0f), ad[m]);
+                } else {
+                    float seg[M];
+                    label_fractions<M>(word, cw, seg);
+#pragma unroll
+                    for (int m = 0; m < M; m++) ad[m] = __fmaf_rn(wr, seg[m], ad[m]);
+                }
             }
-            alpha = __fadd_rn(alpha, step);
+            alpha = an;
+            cx = nx, cy = ny, cz = nz, cbx = nbx, cby = nby, cbz = nbz;
+            w_cur = w_next;
         };
         if (t < t_end && t == 0) {
             sample(0.5f);
@@ -425,32 +463,16 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
         }
         if (cur_m >= 0) store_ad<M>(ad, cur_m, cur_ad);
     } else {
-        // Several volumes (or DRR_FLAG_FULL_MARCH): the reference's step, every volume every step.
+        // Several volumes (or DRR_FLAG_FULL_MARCH): the reference's step. The label cache is keyed by
+        // the last base any enabled volume moved it to (project_kernel.cu:394-431), and a volume whose
+        // base equals the key reads the cached word even if another volume's texture filled it. The
+        // key therefore follows every enabled volume each step, but the word is only fetched when a
+        // contributing volume needs it, from the texture of the volume that set the key: the same
+        // words as the reference's eager fetches, without fetching for volumes that do not count.
+        int key_vol = -1;     // volume whose texture the cached word comes from
+        bool key_ok = false;  // the word of (key_vol, key) has been fetched
         for (; t < t_end; ++t) {
-            float px[NV], py[NV], pz[NV];
-            float seg[NV][M];
-#pragma unroll
-            for (int vol = 0; vol < NV; vol++) {
-#pragma unroll
-                for (int m = 0; m < M; m++) seg[vol][m] = 0.0f;
-                px[vol] = py[vol] = pz[vol] = 0.0f;
-                if (!p.vol[vol].enabled) continue;
-                const float *s = view.vol[vol].s;
-                px[vol] = __fsub_rn(__fmaf_rn(alpha, rxi[vol], s[0]), 1.0f);
-                py[vol] = __fsub_rn(__fmaf_rn(alpha, ryi[vol], s[1]), 1.0f);
-                pz[vol] = __fsub_rn(__fmaf_rn(alpha, rzi[vol], s[2]), 1.0f);
-                const float bx = floorf(px[vol]), by = floorf(py[vol]), bz = floorf(pz[vol]);
-                const float fx = __fsub_rn(px[vol], bx), fy = __fsub_rn(py[vol], by), fz = __fsub_rn(pz[vol], bz);
-                if (bx != pb0 || by != pb1 || bz != pb2) {
-                    word = fetch_label_word(p.vol[vol], bx, by, bz);
-                    pb0 = bx;
-                    pb1 = by;
-                    pb2 = bz;
-                }
-                label_fractions<M>(word, corner_weights(fx, fy, fz), seg[vol]);
-            }
-
-            // priority resolution (project_kernel.cu:458-496)
+            // priority resolution (project_kernel.cu:458-496) needs only alpha
             int cur = NV, n = 0;
 #pragma unroll
             for (int i = 0; i < NV; i++) {
@@ -464,22 +486,44 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
                     n += 1;
                 }
             }
-
+            float weight = 0.0f;
             if (n == 0) {
                 if (attenuate) store_ad<M>(ad, air, add_air(load_ad<M>(ad, air)));
             } else {
-                float weight = __fdiv_rn(1.0f, (float)n);
+                weight = __fdiv_rn(1.0f, (float)n);
                 weight = __fmul_rn(weight, (0 == t || num_steps - 1 == t) ? 0.5f : 1.0f);
+            }
 #pragma unroll
-                for (int vol = 0; vol < NV; vol++) {
-                    // no range re-check, as in project_kernel.cu:541
-                    if (trace[vol] && p.vol[vol].priority == cur) {
-                        const float rho = tex3D<float>(p.vol[vol].density, __fadd_rn(px[vol], 0.5f),
-                                                       __fadd_rn(py[vol], 0.5f), __fadd_rn(pz[vol], 0.5f));
-                        const float wr = __fmul_rn(weight, rho);
+            for (int vol = 0; vol < NV; vol++) {
+                if (!p.vol[vol].enabled) continue;
+                const float *s = view.vol[vol].s;
+                const float px = __fsub_rn(__fmaf_rn(alpha, rxi[vol], s[0]), 1.0f);
+                const float py = __fsub_rn(__fmaf_rn(alpha, ryi[vol], s[1]), 1.0f);
+                const float pz = __fsub_rn(__fmaf_rn(alpha, rzi[vol], s[2]), 1.0f);
+                const float bx = floorf(px), by = floorf(py), bz = floorf(pz);
+                if (bx != pb0 || by != pb1 || bz != pb2) {
+                    pb0 = bx;
+                    pb1 = by;
+                    pb2 = bz;
+                    key_vol = vol;
+                    key_ok = false;
+                }
+                // no range re-check, as in project_kernel.cu:541
+                if (n != 0 && trace[vol] && p.vol[vol].priority == cur) {
+                    if (!key_ok) {
 #pragma unroll
-                        for (int m = 0; m < M; m++) ad[m] = __fmaf_rn(wr, seg[vol][m], ad[m]);
+                        for (int i = 0; i < NV; i++)
+                            if (i == key_vol) word = fetch_label_word(p.vol[i], pb0, pb1, pb2);
+                        key_ok = true;
                     }
+                    float seg[M];
+                    label_fractions<M>(word, corner_weights(__fsub_rn(px, bx), __fsub_rn(py, by), __fsub_rn(pz, bz)),
+                                       seg);
+                    const float rho = tex3D<float>(p.vol[vol].density, __fadd_rn(px, 0.5f), __fadd_rn(py, 0.5f),
+                                                   __fadd_rn(pz, 0.5f));
+                    const float wr = __fmul_rn(weight, rho);
+#pragma unroll
+                    for (int m = 0; m < M; m++) ad[m] = __fmaf_rn(wr, seg[m], ad[m]);
                 }
             }
             alpha = __fadd_rn(alpha, step);
