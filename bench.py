@@ -167,7 +167,7 @@ def run_reference(args, rank: int, world: int):
     if rank != 0:
         return
     vols, projs, kw, name = workload(args, 0)
-    stride = 16 if not args.small else 4
+    stride = 2 if not args.small else 1  # about 10 s of float64 work per step on 16 host cores
     vals = []
     for k in range(args.warmup + args.steps):
         pps, cores, sample = cpu_baseline(vols, [projs[k % len(projs)]], kw, stride=stride)
@@ -465,7 +465,7 @@ def main():
         "e2e": e2e,
     }
     if rank == 0 and not args.no_cpu_baseline:
-        pps, cores, sample = cpu_baseline(vols, projs, kw, stride=16 if not args.small else 4)
+        pps, cores, sample = cpu_baseline(vols, projs, kw, stride=2 if not args.small else 1)
         line["cpu_baseline"] = {"value": pps, "unit": "projections/s", "cores": cores, "kind": "port",
                                 "sample": sample}
     p.free()
