@@ -218,12 +218,10 @@ __global__ void __launch_bounds__(kBlockThreads) adjoint_density_kernel(const __
     const float step = p.step;
     float *const grad = P.grad_density;
     float alpha = R.alpha;
-    // label cell floor(p): its word and material weights
-    float pb0 = __int_as_float(0x7fc00000), pb1 = pb0, pb2 = pb0;
-    bool uni = false;
-    float gu = 0.0f, g8[8];
-#pragma unroll
-    for (int c = 0; c < 8; c++) g8[c] = 0.0f;
+    // label words are loaded one step ahead (as in the forward) so no lane branches to fetch them;
+    // the material weight of a uniform cell is cached while the label stays the same
+    int cur_label = -1;
+    float cur_g = 0.0f;
     // hardware-filter cell and its sums
     int ci = -1, cj = 0, ck = 0, ci1 = 0, cj1 = 0, ck1 = 0;
     float acc[8];
@@ -247,29 +245,55 @@ __global__ void __launch_bounds__(kBlockThreads) adjoint_density_kernel(const __
             acc[c] = 0.0f;
         }
     };
+    float cx = __fsub_rn(__fmaf_rn(alpha, R.rxi, R.sx), 1.0f);
+    float cy = __fsub_rn(__fmaf_rn(alpha, R.ryi, R.sy), 1.0f);
+    float cz = __fsub_rn(__fmaf_rn(alpha, R.rzi, R.sz), 1.0f);
+    float cbx = floorf(cx), cby = floorf(cy), cbz = floorf(cz);
+    uint32_t w_cur = fetch_label_word(V, cbx, cby, cbz);
     for (int t = R.t; t < R.t_end; ++t) {
         const float wt = (0 == t || R.num_steps - 1 == t) ? 0.5f : 1.0f;
-        const float px = __fsub_rn(__fmaf_rn(alpha, R.rxi, R.sx), 1.0f);
-        const float py = __fsub_rn(__fmaf_rn(alpha, R.ryi, R.sy), 1.0f);
-        const float pz = __fsub_rn(__fmaf_rn(alpha, R.rzi, R.sz), 1.0f);
-        const float bx = floorf(px), by = floorf(py), bz = floorf(pz);
-        if (bx != pb0 || by != pb1 || bz != pb2) {
-            const uint32_t word = fetch_label_word(V, bx, by, bz);
-            uni = uniform_word(word);
-            gu = gr_of<M>(R.gr, (int)(word & 15u));
-            if (!uni) {
-#pragma unroll
-                for (int c = 0; c < 8; c++) g8[c] = gr_of<M>(R.gr, (int)((word >> (4 * c)) & 15u));
+        const float an = __fadd_rn(alpha, step);
+        const float nx = __fsub_rn(__fmaf_rn(an, R.rxi, R.sx), 1.0f);
+        const float ny = __fsub_rn(__fmaf_rn(an, R.ryi, R.sy), 1.0f);
+        const float nz = __fsub_rn(__fmaf_rn(an, R.rzi, R.sz), 1.0f);
+        const float nbx = floorf(nx), nby = floorf(ny), nbz = floorf(nz);
+        const uint32_t w_next = fetch_label_word(V, nbx, nby, nbz);
+        const float px = cx, py = cy, pz = cz;
+        const uint32_t word = w_cur;
+        float q;
+        if (uniform_word(word)) {
+            const int L = (int)(word & 15u);
+            if (L != cur_label) {
+                cur_label = L;
+                cur_g = gr_of<M>(R.gr, L);
             }
-            pb0 = bx, pb1 = by, pb2 = bz;
-        }
-        float q = gu;
-        if (!uni) {
-            const CornerWeights cw =
-                corner_weights(__fsub_rn(px, bx), __fsub_rn(py, by), __fsub_rn(pz, bz));
-            q = 0.0f;
+            q = cur_g;
+        } else {
+            const CornerWeights cw = corner_weights(__fsub_rn(px, cbx), __fsub_rn(py, cby), __fsub_rn(pz, cbz));
+            const uint32_t A = word & 15u;
+            const uint32_t xa = word ^ (A * 0x11111111u);
+            const uint32_t B = (word >> ((__ffs(xa) - 1) & ~3)) & 15u;
+            const uint32_t xb = word ^ (B * 0x11111111u);
+            const uint32_t za = ~(((xa & 0x77777777u) + 0x77777777u) | xa) & 0x88888888u;
+            const uint32_t zb = ~(((xb & 0x77777777u) + 0x77777777u) | xb) & 0x88888888u;
+            if ((za | zb) == 0x88888888u) {
+                float sA = 0.0f, sB = 0.0f;
 #pragma unroll
-            for (int c = 0; c < 8; c++) q = __fmaf_rn(__fmul_rn(cw.xy[c & 3], cw.z[c >> 2]), g8[c], q);
+                for (int c = 0; c < 8; c++) {
+                    const float w = __fmul_rn(cw.xy[c & 3], cw.z[c >> 2]);
+                    if ((za >> (4 * c + 3)) & 1u)
+                        sA += w;
+                    else
+                        sB += w;
+                }
+                q = __fmaf_rn(sA, gr_of<M>(R.gr, (int)A), sB * gr_of<M>(R.gr, (int)B));
+            } else {
+                q = 0.0f;
+#pragma unroll
+                for (int c = 0; c < 8; c++)
+                    q = __fmaf_rn(__fmul_rn(cw.xy[c & 3], cw.z[c >> 2]), gr_of<M>(R.gr, (int)((word >> (4 * c)) & 15u)),
+                                  q);
+            }
         }
         int i0, i1, ax_, j0, j1, ay_, k0, k1, az_;
         hw_axis(__fadd_rn(px, 0.5f), n0, i0, i1, ax_);
@@ -288,7 +312,9 @@ __global__ void __launch_bounds__(kBlockThreads) adjoint_density_kernel(const __
         hw_weights(ax_, ay_, az_, W);
 #pragma unroll
         for (int c = 0; c < 8; c++) iw[c] += W[c];
-        alpha = __fadd_rn(alpha, step);
+        alpha = an;
+        cx = nx, cy = ny, cz = nz, cbx = nbx, cby = nby, cbz = nbz;
+        w_cur = w_next;
     }
     if (ci >= 0) flush();
 }
@@ -323,13 +349,11 @@ __global__ void __launch_bounds__(kBlockThreads) adjoint_pose_kernel(const __gri
         float m[7], n[7];
 #pragma unroll
         for (int k = 0; k < 7; k++) m[k] = n[k] = 0.0f;
-        float Hw[3] = {0.f, 0.f, 0.f}, K[3] = {0.f, 0.f, 0.f};
+        // sums of h and alpha h in IJK space; the world-space q = A^T h is applied once per ray
+        float Hi[3] = {0.f, 0.f, 0.f}, Ki[3] = {0.f, 0.f, 0.f};
         auto add_world = [&](float hx, float hy, float hz, float kx, float ky, float kz) {
-#pragma unroll
-            for (int k = 0; k < 3; k++) {
-                Hw[k] += R.A[k] * hx + R.A[3 + k] * hy + R.A[6 + k] * hz;
-                K[k] += R.A[k] * kx + R.A[3 + k] * ky + R.A[6 + k] * kz;
-            }
+            Hi[0] += hx, Hi[1] += hy, Hi[2] += hz;
+            Ki[0] += kx, Ki[1] += ky, Ki[2] += kz;
         };
         auto flush_moments = [&]() {
             if (m[0] == 0.0f) return;
@@ -396,6 +420,12 @@ __global__ void __launch_bounds__(kBlockThreads) adjoint_pose_kernel(const __gri
             alpha = __fadd_rn(alpha, step);
         }
         if (uni) flush_moments();
+        float Hw[3], K[3];
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            Hw[k] = R.A[k] * Hi[0] + R.A[3 + k] * Hi[1] + R.A[6 + k] * Hi[2];
+            K[k] = R.A[k] * Ki[0] + R.A[3 + k] * Ki[1] + R.A[6 + k] * Ki[2];
+        }
         const float d[3] = {P.views[zv].source_world[0] - P.center[0], P.views[zv].source_world[1] - P.center[1],
                             P.views[zv].source_world[2] - P.center[2]};
         const float rr[3] = {R.rx, R.ry, R.rz};
