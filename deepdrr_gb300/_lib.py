@@ -36,7 +36,7 @@ DRR_FLAG_PERSISTENT = 1 << 2
 EXPORTED_SYMBOLS = (
     "drr_volset_create", "drr_volset_destroy", "drr_volset_set_density", "drr_ingest_hu", "drr_tables_create", "drr_tables_destroy",
     "drr_project", "drr_project_adjoint", "drr_graph_create", "drr_graph_set_views", "drr_graph_launch", "drr_graph_destroy",
-    "drr_autotune", "drr_add_noise", "drr_poisson_sample", "drr_neglog", "drr_neglog_noalloc", "drr_clip_upper", "drr_last_error", "drr_version",
+    "drr_autotune", "drr_mesh_area_density", "drr_add_noise", "drr_poisson_sample", "drr_neglog", "drr_neglog_noalloc", "drr_clip_upper", "drr_last_error", "drr_version",
 )
 
 
@@ -69,6 +69,14 @@ class drr_project_args(ctypes.Structure):
         ("intensity", ctypes.c_void_p), ("photon_prob", ctypes.c_void_p),
         ("area_density", ctypes.c_void_p), ("solid_angle", ctypes.c_void_p),
         ("tile_warps_x", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32), ("items_per_grab", ctypes.c_int32),
+        ("mesh_area_density", ctypes.c_void_p), ("n_mesh_slots", ctypes.c_int32), ("mesh_material", ctypes.c_void_p),
+    ]
+
+
+class drr_mesh_desc(ctypes.Structure):
+    _fields_ = [
+        ("triangles", ctypes.c_void_p), ("slot", ctypes.c_void_p), ("density", ctypes.c_void_p),
+        ("n_triangles", ctypes.c_int32), ("n_slots", ctypes.c_int32),
     ]
 
 
@@ -133,6 +141,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     lib.drr_graph_destroy.restype = st
     lib.drr_autotune.argtypes = [vp, vp, ctypes.POINTER(drr_project_args), i32, vp, ctypes.POINTER(drr_tune_result)]
     lib.drr_autotune.restype = st
+    lib.drr_mesh_area_density.argtypes = [ctypes.POINTER(drr_mesh_desc), i32, i32, i32, vp, vp, vp, vp]
+    lib.drr_mesh_area_density.restype = st
     lib.drr_add_noise.argtypes = [vp, vp, vp, i32, i32, i32, ctypes.c_double, ctypes.c_uint64, vp]
     lib.drr_add_noise.restype = st
     lib.drr_poisson_sample.argtypes = [vp, ctypes.c_int64, ctypes.c_uint64, vp, vp]

@@ -46,6 +46,7 @@
 namespace drr {
 
 constexpr int kViewsPerLaunch = 32;
+constexpr int kMaxMeshSlots = 16;
 constexpr int kBlockThreads = 128;  // 4 warps; each warp covers an 8 x 4 pixel tile
 constexpr int kTileW = 16;          // block tile: 16 x 8 pixels
 constexpr int kTileH = 8;
@@ -89,6 +90,9 @@ struct SceneParams {
     float step, max_ray_length;
     int32_t attenuate, air_index;
     int32_t full_march;
+    const float *mesh_ad;                 // [views][n_mesh][H][W] additive mesh integrals (mm g/cm^3) or null
+    int32_t n_mesh;
+    int32_t mesh_mat[kMaxMeshSlots];      // material of each mesh slot
 };
 
 // One launch of the plain kernel: up to kViewsPerLaunch views in the kernel parameters, one block
@@ -456,6 +460,8 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
         }
         const bool last_half = t < t_end && t_end == num_steps;
         const int t_main = last_half ? t_end - 1 : t_end;
+        // two samples per iteration: the loop-carried position and word then need no moves
+#pragma unroll 2
         for (; t < t_main; ++t) sample(1.0f);
         if (last_half) {
             sample(0.5f);
@@ -536,7 +542,19 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
         store_ad<M>(ad, air, (float)((double)a + post));
     }
 #pragma unroll
-    for (int m = 0; m < M; m++) ad[m] = __fdiv_rn(__fmul_rn(ad[m], step), 10.0f);
+    for (int m = 0; m < M; m++) ad[m] = __fmul_rn(ad[m], step);
+    if (p.mesh_ad != nullptr) {
+        // additive meshes (project_kernel.cu:569-579): after the step scaling, before the /10
+        for (int k = 0; k < p.n_mesh; k++) {
+            const float a = p.mesh_ad[(vout * p.n_mesh + k) * plane + pix];
+            const int mm = p.mesh_mat[k];
+#pragma unroll
+            for (int m = 0; m < M; m++)
+                if (m == mm) ad[m] = __fadd_rn(ad[m], a);
+        }
+    }
+#pragma unroll
+    for (int m = 0; m < M; m++) ad[m] = __fdiv_rn(ad[m], 10.0f);
 
     // ---- polychromatic attenuation (project_kernel.cu:637-646) ----
     float inten = 0.0f, prob = 0.0f;

@@ -93,6 +93,9 @@ void fill_scene(drr::SceneParams<NV> &p, const drr_volset *set, const drr_tables
     p.attenuate = (a.flags & DRR_FLAG_ATTENUATE_OUTSIDE) ? 1 : 0;
     p.air_index = a.air_index;
     p.full_march = (a.flags & DRR_FLAG_FULL_MARCH) ? 1 : 0;
+    p.mesh_ad = a.mesh_area_density;
+    p.n_mesh = a.mesh_area_density ? a.n_mesh_slots : 0;
+    for (int k = 0; k < p.n_mesh && k < drr::kMaxMeshSlots; k++) p.mesh_mat[k] = a.mesh_material[k];
 }
 
 template <int NV>
@@ -246,6 +249,13 @@ drr_status validate(const drr_volset *set, const drr_tables *tables, const drr_p
             return fail(DRR_ERR_INVALID_ARGUMENT, "drr_project: priority outside [0, n_volumes)");
     if ((a.flags & DRR_FLAG_ATTENUATE_OUTSIDE) && (a.air_index < 0 || a.air_index >= set->n_materials))
         return fail(DRR_ERR_INVALID_ARGUMENT, "drr_project: air_index outside [0, n_materials)");
+    if (a.mesh_area_density) {
+        if (a.n_mesh_slots < 1 || a.n_mesh_slots > drr::kMaxMeshSlots || !a.mesh_material)
+            return fail(DRR_ERR_INVALID_ARGUMENT, "drr_project: mesh slots outside [1, 16] or no slot materials");
+        for (int k = 0; k < a.n_mesh_slots; k++)
+            if (a.mesh_material[k] < 0 || a.mesh_material[k] >= set->n_materials)
+                return fail(DRR_ERR_INVALID_ARGUMENT, "drr_project: mesh slot material outside [0, n_materials)");
+    }
     return DRR_OK;
 }
 
@@ -388,6 +398,7 @@ extern "C" drr_status drr_graph_create(drr_volset *set, const drr_tables *tables
         free_graph(g);
         return st;
     }
+    g->args.mesh_material = nullptr;     // copied into the captured kernel parameters
     g->args.world_from_index = nullptr;  // the caller's geometry arrays are not kept
     g->args.source_world = nullptr;
     g->args.ijk_from_world = nullptr;

@@ -25,6 +25,7 @@ import numpy as np
 
 from . import _lib, geo
 from .tables import TableSource, build_tables
+from .mesh import Mesh
 from .volume import Volume
 
 log = logging.getLogger(__name__)
@@ -71,11 +72,16 @@ class Projector:
         self.mesh_layers = mesh_layers
         vols = _listify(volume)
         self.volumes: List[Volume] = []
+        self.meshes: List[Mesh] = []
         for v in vols:
             if isinstance(v, Volume):
                 self.volumes.append(v)
+            elif isinstance(v, Mesh):
+                self.meshes.append(v)
             else:
                 raise ValueError(f"unrecognized Renderable type: {type(v)}.")
+        if not self.volumes:
+            raise ValueError("a projector needs at least one volume")
         if priorities is None:
             self.priorities = [len(self.volumes) - 1 - i for i in range(len(self.volumes))]
         else:
@@ -125,9 +131,13 @@ class Projector:
         all_mats = []
         for v in self.volumes:
             all_mats.extend(list(v.materials[0].keys()))
+        for m in self.meshes:  # projector.py:551-552
+            all_mats.append(m.material)
         if attenuate_outside_volume:
             all_mats.append("air")
         self.all_materials = sorted(set(all_mats))
+        # one slot per distinct mesh material, sorted (projector.py:1548-1554)
+        self.mesh_materials = sorted({m.material for m in self.meshes})
         self.air_index = self.all_materials.index("air") if attenuate_outside_volume else 0
         self.attenuate_outside_volume = attenuate_outside_volume
 
@@ -348,12 +358,58 @@ class Projector:
         a.photon_prob = out["photon_prob"].data_ptr() if outputs else None
         a.area_density = out["area_density"].data_ptr() if "area_density" in out else None
         a.solid_angle = out["solid_angle"].data_ptr() if "solid_angle" in out else None
+        if self.meshes:
+            self._mesh_args(a, wfi, src, W0, H0, keep)
         if launch:
             a.tile_warps_x = int(launch.get("tile_warps_x", 0))
             a.blocks_per_sm = int(launch.get("blocks_per_sm", 0))
             a.items_per_grab = int(launch.get("items_per_grab", 0))
         self.output_shape = (W0, H0)
         return a, out
+
+    def _mesh_args(self, a, wfi, src, width, height, keep, stream=None) -> None:
+        """Rasterise the enabled additive meshes for the views of `a` (drr_mesh_area_density) and
+        point `a` at the result."""
+        import torch
+
+        n = wfi.shape[0]
+        S = len(self.mesh_materials)
+        out = torch.empty((n, S, height, width), dtype=torch.float32, device=self.torch_device)
+        tris, slot, dens = self._mesh_triangles()
+        self._mesh_fill(tris, slot, dens, wfi, src, width, height, out, keep, stream)
+        mats = np.asarray([self.all_materials.index(m) for m in self.mesh_materials], dtype=np.int32)
+        keep += [out, mats]
+        a.mesh_area_density = out.data_ptr()
+        a.n_mesh_slots = S
+        a.mesh_material = mats.ctypes.data
+
+    def _mesh_triangles(self):
+        """(triangles [F, 9] float32 world, slot [F] int32, density [F] float32) of the enabled meshes."""
+        meshes = [m for m in self.meshes if m.enabled and len(m.faces)]
+        if not meshes:
+            return np.zeros((0, 9), np.float32), np.zeros(0, np.int32), np.zeros(0, np.float32)
+        tris = np.concatenate([m.triangles_in_world().reshape(-1, 9) for m in meshes]).astype(np.float32)
+        slot = np.concatenate([np.full(len(m.faces), self.mesh_materials.index(m.material), np.int32) for m in meshes])
+        dens = np.concatenate([np.full(len(m.faces), m.density, np.float32) for m in meshes])
+        return tris, slot, dens
+
+    def _mesh_fill(self, tris, slot, dens, wfi, src, width, height, out, keep, stream=None) -> None:
+        import torch
+
+        dev = self.torch_device
+        t_tris = torch.from_numpy(np.ascontiguousarray(tris)).to(dev)
+        t_slot = torch.from_numpy(np.ascontiguousarray(slot)).to(dev)
+        t_dens = torch.from_numpy(np.ascontiguousarray(dens)).to(dev)
+        desc = _lib.drr_mesh_desc()
+        desc.triangles = t_tris.data_ptr() if len(tris) else None
+        desc.slot = t_slot.data_ptr() if len(tris) else None
+        desc.density = t_dens.data_ptr() if len(tris) else None
+        desc.n_triangles = len(tris)
+        desc.n_slots = len(self.mesh_materials)
+        _lib.check(_lib.load().drr_mesh_area_density(ctypes.byref(desc), width, height, wfi.shape[0],
+                                                     wfi.ctypes.data, src.ctypes.data, out.data_ptr(),
+                                                     self._stream_ptr(stream)))
+        keep += [t_tris, t_slot, t_dens]
 
     def _stream_ptr(self, stream):
         import torch
@@ -557,6 +613,12 @@ class ProjectionGraph:
         self._keep = []
         self.args, self.outputs = projector._args(camera_projections, area_density, False,
                                                   _lib.DRR_FLAG_PERSISTENT, launch, self._keep)
+        if projector.meshes:
+            import torch
+
+            n, S = self.args.n_views, len(projector.mesh_materials)
+            buf = [t for t in self._keep if isinstance(t, torch.Tensor) and t.data_ptr() == self.args.mesh_area_density]
+            self.outputs = dict(self.outputs, _mesh_area_density=buf[0])
         self.n_views = self.args.n_views
         handle = ctypes.c_void_p()
         _lib.check(_lib.load().drr_graph_create(projector._volset, projector._tables, ctypes.byref(self.args),
@@ -567,11 +629,16 @@ class ProjectionGraph:
         W0, H0, wfi, src, ijk = self.projector._geometry(camera_projections)
         if wfi.shape[0] != self.n_views or (W0, H0) != (self.args.width, self.args.height):
             raise ValueError("a captured projection keeps its number of views and sensor size")
+        if self.projector.meshes:
+            # the graph reads the mesh integrals from a fixed buffer: rasterise the new views into it
+            out = self.outputs["_mesh_area_density"]
+            tris, slot, dens = self.projector._mesh_triangles()
+            self.projector._mesh_fill(tris, slot, dens, wfi, src, W0, H0, out, self._keep)
         _lib.check(_lib.load().drr_graph_set_views(self._graph, wfi.ctypes.data, src.ctypes.data, ijk.ctypes.data))
 
     def launch(self, stream=None) -> dict:
         _lib.check(_lib.load().drr_graph_launch(self._graph, self.projector._stream_ptr(stream)))
-        return self.outputs
+        return {k: v for k, v in self.outputs.items() if not k.startswith("_")}
 
     def close(self) -> None:
         if self._graph:

@@ -136,7 +136,34 @@ typedef struct {
     int32_t tile_warps_x;           /* 1, 2 or 4 warps across a tile of 4 warps (tiles 8x16, 16x8, 32x4) */
     int32_t blocks_per_sm;          /* resident 128-thread blocks per SM */
     int32_t items_per_grab;         /* tiles a block takes per atomic increment */
+    /* additive meshes (drr_mesh_area_density): per view and mesh-material slot the path integral
+       added to material mesh_material[slot]'s path length before the division by 10
+       (project_kernel.cu:569-579); NULL for none */
+    const float *mesh_area_density; /* device [n_views][n_mesh_slots][H][W], mm g/cm^3 */
+    int32_t n_mesh_slots;
+    const int32_t *mesh_material;   /* host [n_mesh_slots]: material index of each slot */
 } drr_project_args;
+
+/* Triangles of the additive meshes of a projector. */
+typedef struct {
+    const float *triangles; /* device [n_triangles][3][3]: vertices in world coordinates (mm), wound so the
+                               right-handed normal points out of the closed surface */
+    const int32_t *slot;    /* device [n_triangles]: mesh-material slot in [0, n_slots) */
+    const float *density;   /* device [n_triangles]: density of the triangle's mesh (g/cm^3) */
+    int32_t n_triangles;
+    int32_t n_slots;
+} drr_mesh_desc;
+
+/* Path integrals of additive meshes through every pixel of `n_views` views (the views' ray matrices
+ * and sources as in drr_project_args), into `out` (device [n_views][n_slots][H][W], mm g/cm^3):
+ * per slot max(sum of signed distance x density over the surfaces the pixel's centre ray crosses, 0)
+ * where the crossings balance, else 0. Replaces the reference's OpenGL density pass
+ * (pyrenderdrr/renderer.py, shaders/density.frag:9-13) and its read-back (projector.py:1063-1088,
+ * 1302-1330); rasterised in CUDA with 1/256-pixel snapping and a top-left rule, so shared edges
+ * count once. Triangles reaching behind the source are not rasterised. */
+drr_status drr_mesh_area_density(const drr_mesh_desc *mesh, int32_t width, int32_t height, int32_t n_views,
+                                 const double *world_from_index, const double *source_world, float *out,
+                                 void *stream);
 
 /* Render `args->n_views` views into the caller's device buffers, asynchronously on `stream`.
  * Replaces projector.py:709-800 and the projectKernel launch (project_kernel.cu:135-650).

@@ -1,0 +1,94 @@
+"""GPU tests of the additive mesh path (drr_mesh_area_density and its use in drr_project) against
+the oracle's restatement of the reference's density pass (oracle/mesh.py).
+
+Tolerances: the same pixels covered (exact integer coverage); integrals within 1e-6 relative
+(+1e-5 mm g/cm^3: float64 sums in a different order, rounded to float32). In the projector, the mesh
+material's path length moves by the integral / 10 (float32 addition before the division) and no
+other material's changes at all.
+"""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():
+    pytest.skip("needs a CUDA GPU", allow_module_level=True)
+
+import ctypes
+
+import deepdrr_gb300 as dd
+from deepdrr_gb300 import _lib, geo, tables
+from deepdrr_gb300.mesh import Mesh
+from deepdrr_gb300.phantoms import random_views, simple_phantom_hu, volume_from_hu
+from oracle.mesh import mesh_area_density
+
+from helpers import GOLDEN_TABLES
+
+pytestmark = pytest.mark.gpu
+
+
+def gpu_mesh(meshes, projs, n_slots, slot_of):
+    tri = np.concatenate([m.triangles_in_world().reshape(-1, 9) for m in meshes]).astype(np.float32)
+    slot = np.concatenate([np.full(len(m.faces), slot_of[m.material], np.int32) for m in meshes])
+    dens = np.concatenate([np.full(len(m.faces), m.density, np.float32) for m in meshes])
+    views = [geo.view_arrays(p) for p in projs]
+    w, h = views[0][2], views[0][3]
+    wfi = np.ascontiguousarray(np.stack([v[0] for v in views]), dtype=np.float64)
+    src = np.ascontiguousarray(np.stack([v[1] for v in views]), dtype=np.float64)
+    t = [torch.from_numpy(x).cuda() for x in (tri, slot, dens)]
+    out = torch.empty((len(projs), n_slots, h, w), dtype=torch.float32, device="cuda")
+    d = _lib.drr_mesh_desc(t[0].data_ptr(), t[1].data_ptr(), t[2].data_ptr(), len(tri), n_slots)
+    _lib.check(_lib.load().drr_mesh_area_density(ctypes.byref(d), w, h, len(projs), wfi.ctypes.data, src.ctypes.data,
+                                                 out.data_ptr(), None))
+    torch.cuda.synchronize()
+    return out.cpu().numpy(), (tri, slot, dens, wfi, src, w, h)
+
+
+def test_rasterizer_matches_the_oracle():
+    meshes = [Mesh.icosphere(9.0, center=(2.0, -1.0, 3.0), subdivisions=3, material="titanium"),
+              Mesh.box((6.0, 14.0, 5.0), center=(-4.0, 3.0, -2.0), material="iron")]
+    slot_of = {"iron": 0, "titanium": 1}
+    projs = random_views(3, np.zeros(3), seed=3, sphere_mm=3.0, cone_deg=70.0, sensor_size=(72, 56), pixel_size=0.9,
+                         fraction_range=(0.5, 0.6))
+    got, (tri, slot, dens, wfi, src, w, h) = gpu_mesh(meshes, projs, 2, slot_of)
+    for k in range(len(projs)):
+        ref = mesh_area_density(tri, slot, dens, 2, wfi[k], src[k], w, h)
+        assert np.array_equal(got[k] > 0, ref > 0), k
+        np.testing.assert_allclose(got[k], ref, rtol=1e-6, atol=1e-5)
+        assert (ref[1] > 0).sum() > 100 and (ref[0] > 0).sum() > 100
+
+
+def test_projector_adds_the_mesh_to_its_material_only():
+    vol = volume_from_hu(simple_phantom_hu(40, seed=2))
+    mesh = Mesh.icosphere(6.0, center=vol.center_in_world + np.array([3.0, 0.0, 2.0]), material="titanium")
+    projs = random_views(2, vol.center_in_world, seed=5, sphere_mm=2.0, sensor_size=(48, 40), pixel_size=2.0,
+                         fraction_range=(0.5, 0.6))
+    src = tables.NpzTables(GOLDEN_TABLES)
+    kw = dict(spectrum="90KV_AL40", tables=src, neglog=False, step=0.1)
+    with dd.Projector([vol, mesh], **kw) as p:
+        mats = p.all_materials
+        with_mesh = p.project_tensors(*projs, area_density=True)
+        persistent = p.project_tensors(*projs, area_density=True, persistent=True)
+        g = p.capture(*projs, area_density=True)
+        graphed = {k: v.clone() for k, v in g.launch().items()}
+        g.close()
+    assert "titanium" in mats
+    mesh.enabled = False
+    with dd.Projector([vol, mesh], **kw) as p:
+        without = p.project_tensors(*projs, area_density=True)
+    ti = mats.index("titanium")
+    tri = mesh.triangles_in_world().reshape(-1, 9)
+    for k, proj in enumerate(projs):
+        W, s, w, h = geo.view_arrays(proj)
+        add = mesh_area_density(tri, np.zeros(len(tri), np.int32), np.full(len(tri), mesh.density, np.float32), 1,
+                                W, s, w, h)[0]
+        a1 = with_mesh["area_density"][k].cpu().numpy()
+        a0 = without["area_density"][k].cpu().numpy()
+        for m in range(len(mats)):
+            if m != ti:
+                np.testing.assert_array_equal(a1[m], a0[m])
+        # the kernel adds the integral to the step-scaled sum before dividing by 10
+        np.testing.assert_allclose(a1[ti] - a0[ti], add / 10.0, rtol=1e-5, atol=2e-6)
+        assert (add > 0).sum() > 50
+    for k in ("intensity", "photon_prob", "area_density"):
+        assert torch.equal(with_mesh[k], persistent[k]), k
+        assert torch.equal(with_mesh[k], graphed[k]), k
