@@ -156,9 +156,10 @@ def cpu_baseline(vols, projs, kw, stride: int = 16, threads: int = 0):
     ids = (vv * w + uu).ravel().astype(np.int64)
     cores = threads or os.cpu_count() or 1
     t0 = time.perf_counter()
-    sc.project("f64", ray_ids=ids, threads=cores)
+    ref = sc.project("f64", ray_ids=ids, threads=cores)
     dt = time.perf_counter() - t0
     frac = ids.shape[0] / float(w * h)
+    cpu_baseline.last = (ids, ref["intensity"])  # the sample's float64 intensities, for error statements
     return frac / dt, cores, f"{ids.shape[0]} rays (every {stride}th row and column of one {w}x{h} view), " \
                              f"{dt:.2f} s, float64, extrapolated to whole views"
 
@@ -468,6 +469,12 @@ def main():
         pps, cores, sample = cpu_baseline(vols, projs, kw, stride=2 if not args.small else 1)
         line["cpu_baseline"] = {"value": pps, "unit": "projections/s", "cores": cores, "kind": "port",
                                 "sample": sample}
+        # error of this run's first view against the float64 oracle on the same rays
+        ids, ref = cpu_baseline.last
+        got = p.project_tensors(projs[0])["intensity"][0].flatten()[torch.from_numpy(ids).to(f"cuda:{local}")]
+        rel = np.abs(got.double().cpu().numpy() - ref) / np.maximum(np.abs(ref), 1e-12)
+        line["error_vs_float64"] = {"max_rel_intensity": float(rel.max()), "mean_rel_intensity": float(rel.mean()),
+                                    "rays": int(ids.shape[0])}
     p.free()
     if rank == 0:
         print(json.dumps(line), flush=True)

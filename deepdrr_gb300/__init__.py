@@ -8,6 +8,7 @@ reached through the C ABI of ``libdrr_gb300.so`` (``include/drr_gb300.h``).
 from . import geo, tables
 from .device import CameraProjectionDevice, Device, MobileCArm, SimpleDevice
 from .geo import CameraIntrinsicTransform, CameraProjection, FrameTransform
+from .mesh import Mesh
 from .projector import DeprecationError, Projector
 from .volume import Volume, format_materials, hu_to_density, segment_thresholds
 
@@ -15,5 +16,5 @@ __version__ = "0.1.0"
 
 __all__ = [
     "Projector", "Volume", "CameraIntrinsicTransform", "CameraProjection", "FrameTransform",
-    "DeprecationError", "geo", "tables", "Device", "SimpleDevice", "MobileCArm", "CameraProjectionDevice", "hu_to_density", "segment_thresholds", "format_materials",
+    "DeprecationError", "geo", "tables", "Mesh", "Device", "SimpleDevice", "MobileCArm", "CameraProjectionDevice", "hu_to_density", "segment_thresholds", "format_materials",
 ]
