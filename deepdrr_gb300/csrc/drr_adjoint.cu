@@ -5,15 +5,13 @@ namespace drr {
 
 template <int M>
 cudaError_t launch_adjoint(const AdjointParams &p, cudaStream_t stream) {
-    // one warp per ray, eight rays per block, y = view
-    const long long rays = (long long)p.s.width * p.s.height;
-    const dim3 grid((unsigned)((rays + 7) / 8), (unsigned)p.n_views);
+    const dim3 grid((p.s.width + kTileW - 1) / kTileW, (p.s.height + kTileH - 1) / kTileH, p.n_views);
     if (p.grad_density != nullptr) {
-        adjoint_density_kernel<M><<<grid, 256, 0, stream>>>(p);
+        adjoint_density_kernel<M><<<grid, kBlockThreads, 0, stream>>>(p);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
-    if (p.grad_pose != nullptr) adjoint_pose_kernel<M><<<grid, 256, 0, stream>>>(p);
+    if (p.grad_pose != nullptr) adjoint_pose_kernel<M><<<grid, kBlockThreads, 0, stream>>>(p);
     return cudaGetLastError();
 }
 

@@ -111,12 +111,11 @@ struct AdjointRay {
     int t, t_end, num_steps;
 };
 
-// Ray setup identical to render_ray's (single volume), done by all 32 lanes of a warp for the same
-// ray; the spectral sum for the material weights is split over the lanes. Returns false (for the
-// whole warp) when the ray samples nothing or carries no upstream gradient.
+// Ray setup identical to render_ray's (single volume): returns false when the ray samples nothing
+// or carries no upstream gradient.
 template <int M>
-__device__ __forceinline__ bool adjoint_setup_warp(const AdjointParams &P, const AdjointView &av, int u, int v, int zv,
-                                                   int lane, AdjointRay<M> &R) {
+__device__ __forceinline__ bool adjoint_setup(const AdjointParams &P, const AdjointView &av, int u, int v, int zv,
+                                              AdjointRay<M> &R) {
     const SceneParams<1> &p = P.s;
     const ViewRec<1> &view = av.v;
     const VolConst &V = p.vol[0];
@@ -128,12 +127,12 @@ __device__ __forceinline__ bool adjoint_setup_warp(const AdjointParams &P, const
     for (int m = 0; m < M; m++) {
         const size_t at = ((size_t)zv * nmat + m) * plane + pix;
         ad[m] = m < nmat ? P.area_density[at] : 0.0f;
-        R.gr[m] = 0.0f;
+        R.gr[m] = m < nmat && P.grad_area_density != nullptr ? P.grad_area_density[at] : 0.0f;
     }
     const float gI = P.grad_intensity ? P.grad_intensity[zv * plane + pix] : 0.0f;
     const float gP = P.grad_photon_prob ? P.grad_photon_prob[zv * plane + pix] : 0.0f;
     if (gI != 0.0f || gP != 0.0f) {
-        for (int bin = lane; bin < p.n_bins; bin += 32) {
+        for (int bin = 0; bin < p.n_bins; bin++) {
             float x = 0.0f;
 #pragma unroll
             for (int m = 0; m < M; m++)
@@ -149,12 +148,7 @@ __device__ __forceinline__ bool adjoint_setup_warp(const AdjointParams &P, const
     bool any = false;
 #pragma unroll
     for (int m = 0; m < M; m++) {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) R.gr[m] += __shfl_xor_sync(0xffffffffu, R.gr[m], o);
-        const float up = m < nmat && P.grad_area_density != nullptr
-                             ? P.grad_area_density[((size_t)zv * nmat + m) * plane + pix]
-                             : 0.0f;
-        R.gr[m] = (R.gr[m] + up) * scale;
+        R.gr[m] *= scale;
         any |= R.gr[m] != 0.0f;
     }
     if (!any || !V.enabled) return false;
@@ -167,6 +161,8 @@ __device__ __forceinline__ bool adjoint_setup_warp(const AdjointParams &P, const
     R.rx = __fmul_rn(rx, inv_norm);
     R.ry = __fmul_rn(ry, inv_norm);
     R.rz = __fmul_rn(rz, inv_norm);
+    // the rotation in registers: the kernels' atomics could alias the view records as far as the
+    // compiler knows, so reads through the pointer would repeat per sample
 #pragma unroll
     for (int k = 0; k < 9; k++) R.A[k] = view.vol[0].a[k];
     R.rxi = dot3(R.A[0], R.rx, R.A[1], R.ry, R.A[2], R.rz);
@@ -202,172 +198,228 @@ __device__ __forceinline__ bool adjoint_setup_warp(const AdjointParams &P, const
     return R.t < R.t_end;
 }
 
-// First lane of each run of equal keys at or before this lane (keys of a straight ray's cells form
-// contiguous runs: a ray never re-enters a cell it has left).
-__device__ __forceinline__ int run_start(bool head, int lane) {
-    int s = head ? lane : 0;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const int x = __shfl_up_sync(0xffffffffu, s, o);
-        if (lane >= o) s = max(s, x);
-    }
-    return s;
-}
-
-// q = sum_m gr_m seg_m(p) for the sample's label word: the derivative of its contribution by its
-// filtered density (the material weights need only float32 accuracy here, not the forward's
-// rounding order).
+// Density gradient: the exact transpose of the forward's samples. Each sample adds
+// w_t q_t W_c / 256 to texel c of its hardware-filter cell (q_t = sum_m gr_m seg_m). While the cell
+// and w_t q_t stay the same the integer weights W_c are summed and converted once; the cell's eight
+// sums are added to the gradient volume when the ray leaves it.
 template <int M>
-__device__ __forceinline__ float material_weight(uint32_t word, const float gr[M], float fx, float fy, float fz) {
-    if (uniform_word(word)) return gr_of<M>(gr, (int)(word & 15u));
-    const float gx = 1.0f - fx, gy = 1.0f - fy, gz = 1.0f - fz;
-    const float xy[4] = {gx * gy, fx * gy, gx * fy, fx * fy};
-    float q = 0.0f;
-#pragma unroll
-    for (int c = 0; c < 8; c++) q += xy[c & 3] * (c >> 2 ? fz : gz) * gr_of<M>(gr, (int)((word >> (4 * c)) & 15u));
-    return q;
-}
-
-// Density gradient, one warp per ray, lane l on sample t0 + l of each 32-sample chunk: the exact
-// transpose of the forward's samples. Each sample adds w_t q_t W_c / 256 to texel c of its
-// hardware-filter cell; lanes in the same cell sum their eight values by a segmented warp scan and
-// the last lane of each run adds the sums to the gradient volume.
-template <int M>
-__global__ void __launch_bounds__(256) adjoint_density_kernel(const __grid_constant__ AdjointParams P) {
+__global__ void __launch_bounds__(kBlockThreads) adjoint_density_kernel(const __grid_constant__ AdjointParams P) {
     const SceneParams<1> &p = P.s;
     const int lane = threadIdx.x & 31;
-    const int ray = blockIdx.x * 8 + (threadIdx.x >> 5);
-    const int zv = blockIdx.y;
-    if (ray >= p.width * p.height || zv >= P.n_views) return;  // whole warps
-    const int u = ray % p.width, v = ray / p.width;
+    const int warp = threadIdx.x >> 5;
+    const int u = blockIdx.x * kTileW + ((warp & 1) << 3) + (lane & 7);
+    const int v = blockIdx.y * kTileH + ((warp >> 1) << 2) + (lane >> 3);
+    const int zv = blockIdx.z;
+    if (u >= p.width || v >= p.height || zv >= P.n_views) return;
     AdjointRay<M> R;
-    if (!adjoint_setup_warp<M>(P, P.views[zv], u, v, zv, lane, R)) return;
+    if (!adjoint_setup<M>(P, P.views[zv], u, v, zv, R)) return;
     const VolConst &V = p.vol[0];
     const int n0 = V.n[0], n1 = V.n[1], n2 = V.n[2];
     const float step = p.step;
     float *const grad = P.grad_density;
-    float chunk_alpha = R.alpha;
-    for (int t0 = R.t; t0 < R.t_end; t0 += 32) {
-        const int t = t0 + lane;
-        const float alpha = alpha_after(chunk_alpha, step, lane);
-        const float wt = t >= R.t_end ? 0.0f : ((0 == t || R.num_steps - 1 == t) ? 0.5f : 1.0f);
-        const float px = __fsub_rn(__fmaf_rn(alpha, R.rxi, R.sx), 1.0f);
-        const float py = __fsub_rn(__fmaf_rn(alpha, R.ryi, R.sy), 1.0f);
-        const float pz = __fsub_rn(__fmaf_rn(alpha, R.rzi, R.sz), 1.0f);
-        const float bx = floorf(px), by = floorf(py), bz = floorf(pz);
-        const uint32_t word = fetch_label_word(V, bx, by, bz);
-        const float q = material_weight<M>(word, R.gr, px - bx, py - by, pz - bz);
+    float alpha = R.alpha;
+    // label words are loaded one step ahead (as in the forward) so no lane branches to fetch them;
+    // the material weight of a uniform cell is cached while the label stays the same
+    int cur_label = -1;
+    float cur_g = 0.0f;
+    // hardware-filter cell and its sums
+    int ci = -1, cj = 0, ck = 0, ci1 = 0, cj1 = 0, ck1 = 0;
+    float acc[8];
+    int iw[8];
+#pragma unroll
+    for (int c = 0; c < 8; c++) acc[c] = 0.0f, iw[c] = 0;
+    float run = 0.0f;  // w_t q_t / 256 of the integer sums in iw
+    auto fold = [&]() {
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+            acc[c] = __fmaf_rn(run, (float)iw[c], acc[c]);
+            iw[c] = 0;
+        }
+    };
+    auto flush = [&]() {
+        fold();
+        const int is[2] = {ci, ci1}, js[2] = {cj, cj1}, ks[2] = {ck, ck1};
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+            if (acc[c] != 0.0f) atomicAdd(grad + ((size_t)ks[c >> 2] * n1 + js[(c >> 1) & 1]) * n0 + is[c & 1], acc[c]);
+            acc[c] = 0.0f;
+        }
+    };
+    float cx = __fsub_rn(__fmaf_rn(alpha, R.rxi, R.sx), 1.0f);
+    float cy = __fsub_rn(__fmaf_rn(alpha, R.ryi, R.sy), 1.0f);
+    float cz = __fsub_rn(__fmaf_rn(alpha, R.rzi, R.sz), 1.0f);
+    float cbx = floorf(cx), cby = floorf(cy), cbz = floorf(cz);
+    uint32_t w_cur = fetch_label_word(V, cbx, cby, cbz);
+    for (int t = R.t; t < R.t_end; ++t) {
+        const float wt = (0 == t || R.num_steps - 1 == t) ? 0.5f : 1.0f;
+        const float an = __fadd_rn(alpha, step);
+        const float nx = __fsub_rn(__fmaf_rn(an, R.rxi, R.sx), 1.0f);
+        const float ny = __fsub_rn(__fmaf_rn(an, R.ryi, R.sy), 1.0f);
+        const float nz = __fsub_rn(__fmaf_rn(an, R.rzi, R.sz), 1.0f);
+        const float nbx = floorf(nx), nby = floorf(ny), nbz = floorf(nz);
+        const uint32_t w_next = fetch_label_word(V, nbx, nby, nbz);
+        const float px = cx, py = cy, pz = cz;
+        const uint32_t word = w_cur;
+        float q;
+        if (uniform_word(word)) {
+            const int L = (int)(word & 15u);
+            if (L != cur_label) {
+                cur_label = L;
+                cur_g = gr_of<M>(R.gr, L);
+            }
+            q = cur_g;
+        } else {
+            const CornerWeights cw = corner_weights(__fsub_rn(px, cbx), __fsub_rn(py, cby), __fsub_rn(pz, cbz));
+            const uint32_t A = word & 15u;
+            const uint32_t xa = word ^ (A * 0x11111111u);
+            const uint32_t B = (word >> ((__ffs(xa) - 1) & ~3)) & 15u;
+            const uint32_t xb = word ^ (B * 0x11111111u);
+            const uint32_t za = ~(((xa & 0x77777777u) + 0x77777777u) | xa) & 0x88888888u;
+            const uint32_t zb = ~(((xb & 0x77777777u) + 0x77777777u) | xb) & 0x88888888u;
+            if ((za | zb) == 0x88888888u) {
+                float sA = 0.0f, sB = 0.0f;
+#pragma unroll
+                for (int c = 0; c < 8; c++) {
+                    const float w = __fmul_rn(cw.xy[c & 3], cw.z[c >> 2]);
+                    if ((za >> (4 * c + 3)) & 1u)
+                        sA += w;
+                    else
+                        sB += w;
+                }
+                q = __fmaf_rn(sA, gr_of<M>(R.gr, (int)A), sB * gr_of<M>(R.gr, (int)B));
+            } else {
+                q = 0.0f;
+#pragma unroll
+                for (int c = 0; c < 8; c++)
+                    q = __fmaf_rn(__fmul_rn(cw.xy[c & 3], cw.z[c >> 2]), gr_of<M>(R.gr, (int)((word >> (4 * c)) & 15u)),
+                                  q);
+            }
+        }
         int i0, i1, ax_, j0, j1, ay_, k0, k1, az_;
         hw_axis(__fadd_rn(px, 0.5f), n0, i0, i1, ax_);
         hw_axis(__fadd_rn(py, 0.5f), n1, j0, j1, ay_);
         hw_axis(__fadd_rn(pz, 0.5f), n2, k0, k1, az_);
+        if (i0 != ci || j0 != cj || k0 != ck) {
+            if (ci >= 0) flush();
+            ci = i0, cj = j0, ck = k0, ci1 = i1, cj1 = j1, ck1 = k1;
+        }
+        const float r = wt * q * (1.0f / 256.0f);
+        if (r != run) {
+            fold();
+            run = r;
+        }
         int W[8];
         hw_weights(ax_, ay_, az_, W);
-        const float r = wt * q * (1.0f / 256.0f);
-        float c8[8];
 #pragma unroll
-        for (int c = 0; c < 8; c++) c8[c] = r * (float)W[c];
-        // runs of lanes in the same filter cell
-        const int pi = __shfl_up_sync(0xffffffffu, i0, 1), pj = __shfl_up_sync(0xffffffffu, j0, 1),
-                  pk = __shfl_up_sync(0xffffffffu, k0, 1);
-        const bool head = lane == 0 || pi != i0 || pj != j0 || pk != k0;
-        const int s = run_start(head, lane);
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-#pragma unroll
-            for (int c = 0; c < 8; c++) {
-                const float x = __shfl_up_sync(0xffffffffu, c8[c], o);
-                if (lane - o >= s) c8[c] += x;
-            }
-        }
-        const bool next_head = __shfl_down_sync(0xffffffffu, head ? 1 : 0, 1) != 0;
-        if (lane == 31 || next_head) {
-            const int is[2] = {i0, i1}, js[2] = {j0, j1}, ks[2] = {k0, k1};
-#pragma unroll
-            for (int c = 0; c < 8; c++)
-                if (c8[c] != 0.0f) atomicAdd(grad + ((size_t)ks[c >> 2] * n1 + js[(c >> 1) & 1]) * n0 + is[c & 1], c8[c]);
-        }
-        chunk_alpha = __fadd_rn(__shfl_sync(0xffffffffu, alpha, 31), step);
+        for (int c = 0; c < 8; c++) iw[c] += W[c];
+        alpha = an;
+        cx = nx, cy = ny, cz = nz, cbx = nbx, cby = nby, cbz = nbz;
+        w_cur = w_next;
     }
+    if (ci >= 0) flush();
 }
 
-// Pose gradient, one warp per ray as above: h = d/dp of w_t rho(p) Q(p) with rho and Q the
-// continuous trilinear interpolants of the label cell's texels and per-corner material weights.
-// The first lane of each run of lanes in one label cell fetches the cell's eight texels; shuffles
-// hand them to the run. h and alpha h are summed in IJK space and rotated to the world once.
+// Pose gradient: d/dp of w_t rho(p) Q(p) with rho and Q the continuous trilinear interpolants of the
+// label cell's texels and per-corner material weights, summed as q_w = A^T h (Hw) and alpha q_w (K).
+// In a cell whose eight labels agree Q is constant and grad rho is bilinear in the fractions, so the
+// cell's samples are summed as weighted moments of the fractions and turned into h when the ray
+// leaves the cell; mixed cells are evaluated per sample.
 template <int M>
-__global__ void __launch_bounds__(256) adjoint_pose_kernel(const __grid_constant__ AdjointParams P) {
-    __shared__ float s_pose[8][6];
+__global__ void __launch_bounds__(kBlockThreads) adjoint_pose_kernel(const __grid_constant__ AdjointParams P) {
     const SceneParams<1> &p = P.s;
     const int lane = threadIdx.x & 31;
-    const int wib = threadIdx.x >> 5;
-    const int ray = blockIdx.x * 8 + wib;
-    const int zv = blockIdx.y;
+    const int warp = threadIdx.x >> 5;
+    const int u = blockIdx.x * kTileW + ((warp & 1) << 3) + (lane & 7);
+    const int v = blockIdx.y * kTileH + ((warp >> 1) << 2) + (lane >> 3);
+    const int zv = blockIdx.z;
+    const bool active = u < p.width && v < p.height && zv < P.n_views;
     float pose[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     AdjointRay<M> R;
-    if (ray < p.width * p.height && zv < P.n_views &&
-        adjoint_setup_warp<M>(P, P.views[zv], ray % p.width, ray / p.width, zv, lane, R)) {
+    if (active && adjoint_setup<M>(P, P.views[zv], u, v, zv, R)) {
         const VolConst &V = p.vol[0];
         const float step = p.step;
+        float alpha = R.alpha;
+        float pb0 = __int_as_float(0x7fc00000), pb1 = pb0, pb2 = pb0;
+        bool uni = false;
+        float gu = 0.0f, g8[8], rho8[8];
+#pragma unroll
+        for (int c = 0; c < 8; c++) g8[c] = rho8[c] = 0.0f;
+        // moments of the current uniform cell: sum w, w f_x, w f_y, w f_z, w f_x f_y, w f_x f_z,
+        // w f_y f_z, and the same weighted by alpha
+        float m[7], n[7];
+#pragma unroll
+        for (int k = 0; k < 7; k++) m[k] = n[k] = 0.0f;
+        // sums of h and alpha h in IJK space; the world-space q = A^T h is applied once per ray
         float Hi[3] = {0.f, 0.f, 0.f}, Ki[3] = {0.f, 0.f, 0.f};
-        float chunk_alpha = R.alpha;
-        for (int t0 = R.t; t0 < R.t_end; t0 += 32) {
-            const int t = t0 + lane;
-            const float alpha = alpha_after(chunk_alpha, step, lane);
-            const float wt = t >= R.t_end ? 0.0f : ((0 == t || R.num_steps - 1 == t) ? 0.5f : 1.0f);
+        auto add_world = [&](float hx, float hy, float hz, float kx, float ky, float kz) {
+            Hi[0] += hx, Hi[1] += hy, Hi[2] += hz;
+            Ki[0] += kx, Ki[1] += ky, Ki[2] += kz;
+        };
+        auto flush_moments = [&]() {
+            if (m[0] == 0.0f) return;
+            const float *r = rho8;
+            const float dx0 = r[1] - r[0], dx1 = r[3] - r[2], dx2 = r[5] - r[4], dx3 = r[7] - r[6];
+            const float dy0 = r[2] - r[0], dy1 = r[3] - r[1], dy2 = r[6] - r[4], dy3 = r[7] - r[5];
+            const float dz0 = r[4] - r[0], dz1 = r[5] - r[1], dz2 = r[6] - r[2], dz3 = r[7] - r[3];
+            // d rho / d f_x = dx0 + (dx1 - dx0) f_y + (dx2 - dx0) f_z + (dx0 - dx1 - dx2 + dx3) f_y f_z, etc.
+            auto gsum = [&](const float *s) {
+                float g[3];
+                g[0] = dx0 * s[0] + (dx1 - dx0) * s[2] + (dx2 - dx0) * s[3] + (dx0 - dx1 - dx2 + dx3) * s[6];
+                g[1] = dy0 * s[0] + (dy1 - dy0) * s[1] + (dy2 - dy0) * s[3] + (dy0 - dy1 - dy2 + dy3) * s[5];
+                g[2] = dz0 * s[0] + (dz1 - dz0) * s[1] + (dz2 - dz0) * s[2] + (dz0 - dz1 - dz2 + dz3) * s[4];
+                return make_float3(g[0] * gu, g[1] * gu, g[2] * gu);
+            };
+            const float3 h = gsum(m), hk = gsum(n);
+            add_world(h.x, h.y, h.z, hk.x, hk.y, hk.z);
+#pragma unroll
+            for (int k = 0; k < 7; k++) m[k] = n[k] = 0.0f;
+        };
+        for (int t = R.t; t < R.t_end; ++t) {
+            const float wt = (0 == t || R.num_steps - 1 == t) ? 0.5f : 1.0f;
             const float px = __fsub_rn(__fmaf_rn(alpha, R.rxi, R.sx), 1.0f);
             const float py = __fsub_rn(__fmaf_rn(alpha, R.ryi, R.sy), 1.0f);
             const float pz = __fsub_rn(__fmaf_rn(alpha, R.rzi, R.sz), 1.0f);
             const float bx = floorf(px), by = floorf(py), bz = floorf(pz);
-            const float fx = px - bx, fy = py - by, fz = pz - bz;
-            const float gx = 1.0f - fx, gy = 1.0f - fy, gz = 1.0f - fz;
-            const float qx = __shfl_up_sync(0xffffffffu, bx, 1), qy = __shfl_up_sync(0xffffffffu, by, 1),
-                        qz = __shfl_up_sync(0xffffffffu, bz, 1);
-            const bool head = lane == 0 || qx != bx || qy != by || qz != bz;
-            const int s = run_start(head, lane);
-            float rho8[8];
+            const float fx = __fsub_rn(px, bx), fy = __fsub_rn(py, by), fz = __fsub_rn(pz, bz);
+            if (bx != pb0 || by != pb1 || bz != pb2) {
+                if (uni) flush_moments();
+                const uint32_t word = fetch_label_word(V, bx, by, bz);
+                uni = uniform_word(word);
+                gu = gr_of<M>(R.gr, (int)(word & 15u));
+                if (!uni) {
 #pragma unroll
-            for (int c = 0; c < 8; c++) {
-                float r = 0.0f;
-                if (head)
-                    r = tex3D<float>(P.density_point, bx + (float)(c & 1) + 0.5f, by + (float)((c >> 1) & 1) + 0.5f,
-                                     bz + (float)(c >> 2) + 0.5f);
-                rho8[c] = __shfl_sync(0xffffffffu, r, s);
+                    for (int c = 0; c < 8; c++) g8[c] = gr_of<M>(R.gr, (int)((word >> (4 * c)) & 15u));
+                }
+#pragma unroll
+                for (int c = 0; c < 8; c++)
+                    rho8[c] = tex3D<float>(P.density_point, bx + (float)(c & 1) + 0.5f,
+                                           by + (float)((c >> 1) & 1) + 0.5f, bz + (float)(c >> 2) + 0.5f);
+                pb0 = bx, pb1 = by, pb2 = bz;
             }
-            const uint32_t word = fetch_label_word(V, bx, by, bz);
-            float dr[3];
-            trilinear_grad(rho8, fx, fy, fz, gx, gy, gz, dr);
-            float h[3];
-            if (uniform_word(word)) {
-                const float wQ = wt * gr_of<M>(R.gr, (int)(word & 15u));
-                h[0] = wQ * dr[0], h[1] = wQ * dr[1], h[2] = wQ * dr[2];
+            if (uni) {
+                if (gu != 0.0f) {
+                    const float wa = wt * alpha;
+                    const float fxy = fx * fy, fxz = fx * fz, fyz = fy * fz;
+                    m[0] += wt, m[1] += wt * fx, m[2] += wt * fy, m[3] += wt * fz;
+                    m[4] += wt * fxy, m[5] += wt * fxz, m[6] += wt * fyz;
+                    n[0] += wa, n[1] += wa * fx, n[2] += wa * fy, n[3] += wa * fz;
+                    n[4] += wa * fxy, n[5] += wa * fxz, n[6] += wa * fyz;
+                }
             } else {
-                float g8[8];
-#pragma unroll
-                for (int c = 0; c < 8; c++) g8[c] = gr_of<M>(R.gr, (int)((word >> (4 * c)) & 15u));
-                float dQ[3];
+                const float gx = 1.0f - fx, gy = 1.0f - fy, gz = 1.0f - fz;
+                float dr[3], dQ[3];
+                trilinear_grad(rho8, fx, fy, fz, gx, gy, gz, dr);
                 trilinear_grad(g8, fx, fy, fz, gx, gy, gz, dQ);
                 const float rho = trilinear(rho8, fx, fy, fz, gx, gy, gz);
                 const float Q = trilinear(g8, fx, fy, fz, gx, gy, gz);
-                h[0] = wt * (dr[0] * Q + rho * dQ[0]);
-                h[1] = wt * (dr[1] * Q + rho * dQ[1]);
-                h[2] = wt * (dr[2] * Q + rho * dQ[2]);
+                const float hx = wt * (dr[0] * Q + rho * dQ[0]);
+                const float hy = wt * (dr[1] * Q + rho * dQ[1]);
+                const float hz = wt * (dr[2] * Q + rho * dQ[2]);
+                add_world(hx, hy, hz, alpha * hx, alpha * hy, alpha * hz);
             }
-#pragma unroll
-            for (int k = 0; k < 3; k++) {
-                Hi[k] += h[k];
-                Ki[k] = __fmaf_rn(alpha, h[k], Ki[k]);
-            }
-            chunk_alpha = __fadd_rn(__shfl_sync(0xffffffffu, alpha, 31), step);
+            alpha = __fadd_rn(alpha, step);
         }
-#pragma unroll
-        for (int k = 0; k < 3; k++) {
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                Hi[k] += __shfl_xor_sync(0xffffffffu, Hi[k], o);
-                Ki[k] += __shfl_xor_sync(0xffffffffu, Ki[k], o);
-            }
-        }
+        if (uni) flush_moments();
         float Hw[3], K[3];
 #pragma unroll
         for (int k = 0; k < 3; k++) {
@@ -384,16 +436,14 @@ __global__ void __launch_bounds__(256) adjoint_pose_kernel(const __grid_constant
         pose[4] = -((d[2] * Hw[0] - d[0] * Hw[2]) + (rr[2] * K[0] - rr[0] * K[2]));
         pose[5] = -((d[0] * Hw[1] - d[1] * Hw[0]) + (rr[0] * K[1] - rr[1] * K[0]));
     }
-    // one ray per warp: lane 0 holds its ray's terms; sum the block's eight rays, one atomic each
-    if (lane == 0) {
+    if (zv < P.n_views) {
+        // one view per block: reduce over the warp, then one atomic per warp and component
 #pragma unroll
-        for (int k = 0; k < 6; k++) s_pose[wib][k] = pose[k];
-    }
-    __syncthreads();
-    if (threadIdx.x < 6 && zv < P.n_views) {
-        float x = 0.0f;
-        for (int w = 0; w < 8; w++) x += s_pose[w][threadIdx.x];
-        if (x != 0.0f) atomicAdd(P.grad_pose + (size_t)zv * 6 + threadIdx.x, x);
+        for (int k = 0; k < 6; k++) {
+            float x = pose[k];
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+            if (lane == 0 && x != 0.0f) atomicAdd(P.grad_pose + (size_t)zv * 6 + k, x);
+        }
     }
 }
 

@@ -11,7 +11,6 @@
 // and in the CPU test that compares it with the serial loop.
 #pragma once
 
-#include <math.h>
 #include <stdint.h>
 #include <string.h>
 
@@ -150,38 +149,6 @@ DRR_HD int advance_alpha(float *alpha, float step, float bound, int limit, bool 
     }
     *alpha = a;
     return k;
-}
-
-// alpha after k >= 0 further float32 additions of step: the same value as k serial additions. When
-// the k additions stay inside alpha's binade (and no rounding tie depends on alpha's last bit) every
-// addition adds the same number of ulps, so the result is one integer multiply-add on the bits;
-// otherwise advance_alpha.
-DRR_HD float alpha_after(float a, float step, int k) {
-    if (k <= 0) return a;
-    const uint32_t abits = float_bits(a), sbits = float_bits(step);
-    const int aexp = (int)((abits >> 23) & 0xff), sexp = (int)((sbits >> 23) & 0xff);
-    if ((abits >> 31) == 0 && aexp != 0 && aexp < 0xfe && sexp != 0 && sexp != 0xff && (sbits >> 31) == 0) {
-        const int64_t am = (int64_t)((abits & 0x7fffff) | 0x800000);
-        const int64_t smant = (int64_t)((sbits & 0x7fffff) | 0x800000);
-        const int sh = aexp - sexp;
-        int64_t delta = -1;
-        if (sh <= 0 && sh >= -30) {
-            delta = smant << (-sh);
-        } else if (sh > 0 && sh <= 62) {
-            const int64_t m = smant >> sh, rem = smant - (m << sh), half = (int64_t)1 << (sh - 1);
-            if (rem < half)
-                delta = m;
-            else if (rem > half)
-                delta = m + 1;
-            else if ((am & 1) == 0)
-                delta = m + (m & 1);
-        }
-        if (delta > 0 && am + (int64_t)k * delta <= ((int64_t)1 << 24) - 2)
-            return bits_float((uint32_t)(aexp << 23) | (uint32_t)((am + (int64_t)k * delta) & 0x7fffff));
-    }
-    float b = a;
-    advance_alpha(&b, step, INFINITY, k, false);
-    return b;
 }
 
 }  // namespace drr

@@ -16,5 +16,3 @@ extern "C" int serial(float *alpha, float step, float bound, int limit, int incl
     *alpha = a;
     return k;
 }
-
-extern "C" float alpha_after(float alpha, float step, int k) { return drr::alpha_after(alpha, step, k); }

@@ -66,19 +66,3 @@ def test_ties_and_binade_edges(shim):
                         ff, se = _both(shim, float(np.float32(a0)), float(np.float32(step)),
                                        float(np.float32(bound)), 50000, inclusive)
                         assert ff[0] == se[0] and ff[1].tobytes() == se[1].tobytes(), (e, step, a0, bound, ff, se)
-
-
-def test_alpha_after_matches_serial_additions(shim):
-    """alpha_after (the adjoint's per-lane alpha) against k serial float32 additions."""
-    shim.alpha_after.restype = ctypes.c_float
-    shim.alpha_after.argtypes = [ctypes.c_float, ctypes.c_float, ctypes.c_int]
-    rng = np.random.default_rng(7)
-    for _ in range(3000):
-        a0 = np.float32(rng.choice([rng.uniform(0.5, 2.0), rng.uniform(1, 1600), 2.0 ** rng.integers(-3, 11)]))
-        step = np.float32(rng.choice([0.1, 0.05, 0.2, 0.025, 1.0, 0.3, rng.uniform(0.01, 1.0)]))
-        k = int(rng.integers(0, 32))
-        want = a0
-        for _ in range(k):
-            want = np.float32(want + step)
-        got = np.float32(shim.alpha_after(float(a0), float(step), k))
-        assert got == want, (a0, step, k, got, want)
