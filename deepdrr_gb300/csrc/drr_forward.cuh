@@ -223,6 +223,26 @@ __device__ __forceinline__ void label_fractions(uint32_t word, const CornerWeigh
 #pragma unroll
         for (int m = 0; m < M; m++)
             if (m == L) seg[m] = s;
+        return;
+    }
+    // two labels A (corner 0's) and B: one pass over the corners into two sums, each in corner order
+    const uint32_t A = word & 15u;
+    const uint32_t xa = word ^ (A * 0x11111111u);
+    const uint32_t B = (word >> ((__ffs(xa) - 1) & ~3)) & 15u;
+    const uint32_t xb = word ^ (B * 0x11111111u);
+    const uint32_t za = ~(((xa & 0x77777777u) + 0x77777777u) | xa) & 0x88888888u;  // nibbles equal to A
+    const uint32_t zb = ~(((xb & 0x77777777u) + 0x77777777u) | xb) & 0x88888888u;  // nibbles equal to B
+    if ((za | zb) == 0x88888888u) {
+        float sA = 0.0f, sB = 0.0f;
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+            if ((za >> (4 * c + 3)) & 1u)
+                sA = __fmaf_rn(cw.xy[c & 3], cw.z[c >> 2], sA);
+            else
+                sB = __fmaf_rn(cw.xy[c & 3], cw.z[c >> 2], sB);
+        }
+#pragma unroll
+        for (int m = 0; m < M; m++) seg[m] = (uint32_t)m == A ? sA : ((uint32_t)m == B ? sB : 0.0f);
     } else {
 #pragma unroll
         for (int c = 0; c < 8; c++) {
