@@ -26,6 +26,9 @@ DRR_HU_I16 = 1
 DRR_HU_F64 = 2
 
 DRR_MAX_VOLUMES = 4
+DRR_MAX_MESH_LAYERS = 4
+DRR_MESH_ADDITIVE = 1
+DRR_MESH_SUBTRACTIVE = 2
 DRR_MAX_MATERIALS = 16
 
 DRR_FLAG_ATTENUATE_OUTSIDE = 1 << 0
@@ -36,7 +39,7 @@ DRR_FLAG_PERSISTENT = 1 << 2
 EXPORTED_SYMBOLS = (
     "drr_volset_create", "drr_volset_destroy", "drr_volset_set_density", "drr_ingest_hu", "drr_tables_create", "drr_tables_destroy",
     "drr_project", "drr_project_adjoint", "drr_graph_create", "drr_graph_set_views", "drr_graph_launch", "drr_graph_destroy",
-    "drr_autotune", "drr_mesh_area_density", "drr_add_noise", "drr_poisson_sample", "drr_neglog", "drr_neglog_noalloc", "drr_clip_upper", "drr_last_error", "drr_version",
+    "drr_autotune", "drr_mesh_hits", "drr_mesh_area_density", "drr_add_noise", "drr_poisson_sample", "drr_neglog", "drr_neglog_noalloc", "drr_clip_upper", "drr_last_error", "drr_version",
 )
 
 
@@ -70,13 +73,16 @@ class drr_project_args(ctypes.Structure):
         ("area_density", ctypes.c_void_p), ("solid_angle", ctypes.c_void_p),
         ("tile_warps_x", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32), ("items_per_grab", ctypes.c_int32),
         ("mesh_area_density", ctypes.c_void_p), ("n_mesh_slots", ctypes.c_int32), ("mesh_material", ctypes.c_void_p),
+        ("mesh_hit_alpha", ctypes.c_void_p), ("mesh_hit_facing", ctypes.c_void_p),
+        ("mesh_hit_layers", ctypes.c_int32), ("max_mesh_hits", ctypes.c_int32),
     ]
 
 
 class drr_mesh_desc(ctypes.Structure):
     _fields_ = [
         ("triangles", ctypes.c_void_p), ("slot", ctypes.c_void_p), ("density", ctypes.c_void_p),
-        ("n_triangles", ctypes.c_int32), ("n_slots", ctypes.c_int32),
+        ("layer", ctypes.c_void_p), ("mode", ctypes.c_void_p),
+        ("n_triangles", ctypes.c_int32), ("n_slots", ctypes.c_int32), ("n_layers", ctypes.c_int32),
     ]
 
 
@@ -141,7 +147,9 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     lib.drr_graph_destroy.restype = st
     lib.drr_autotune.argtypes = [vp, vp, ctypes.POINTER(drr_project_args), i32, vp, ctypes.POINTER(drr_tune_result)]
     lib.drr_autotune.restype = st
-    lib.drr_mesh_area_density.argtypes = [ctypes.POINTER(drr_mesh_desc), i32, i32, i32, vp, vp, vp, vp]
+    lib.drr_mesh_hits.argtypes = [ctypes.POINTER(drr_mesh_desc), i32, i32, vp, vp, i32, vp, vp, vp]
+    lib.drr_mesh_hits.restype = st
+    lib.drr_mesh_area_density.argtypes = [ctypes.POINTER(drr_mesh_desc), i32, i32, i32, vp, vp, vp, vp, i32, vp, vp]
     lib.drr_mesh_area_density.restype = st
     lib.drr_add_noise.argtypes = [vp, vp, vp, i32, i32, i32, ctypes.c_double, ctypes.c_uint64, vp]
     lib.drr_add_noise.restype = st

@@ -47,6 +47,7 @@ namespace drr {
 
 constexpr int kViewsPerLaunch = 32;
 constexpr int kMaxMeshSlots = 16;
+constexpr int kMaxMeshLayers = 4;
 constexpr int kBlockThreads = 128;  // 4 warps; each warp covers an 8 x 4 pixel tile
 constexpr int kTileW = 16;          // block tile: 16 x 8 pixels
 constexpr int kTileH = 8;
@@ -93,6 +94,9 @@ struct SceneParams {
     const float *mesh_ad;                 // [views][n_mesh][H][W] additive mesh integrals (mm g/cm^3) or null
     int32_t n_mesh;
     int32_t mesh_mat[kMaxMeshSlots];      // material of each mesh slot
+    const float *hit_alpha;               // [hit_layers][H][W][max_hits] subtractive crossings (one view) or null
+    const int8_t *hit_facing;
+    int32_t hit_layers, max_hits;
 };
 
 // One launch of the plain kernel: up to kViewsPerLaunch views in the kernel parameters, one block
@@ -367,7 +371,8 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
     float alpha = minA;
     int t = 0;
     int t_end = num_steps;  // the march can stop here: no interval is open beyond it
-    if (!p.full_march) {
+    const bool carve = p.hit_alpha != nullptr;  // subtractive meshes: the reference's full march
+    if (!p.full_march && !carve) {
         // Skip the steps before any interval opens and stop after the last one closes; the float32
         // alpha sequence is fast-forwarded exactly (drr_alpha.h), so later positions are unchanged.
         if (amin <= amax) {
@@ -392,7 +397,7 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
     float pb0 = __int_as_float(0x7fc00000), pb1 = pb0, pb2 = pb0;  // previous_coordinates (none yet)
     uint32_t word = 0;
 
-    if (NV == 1 && !p.full_march) {
+    if (NV == 1 && !p.full_march && !carve) {
         // One volume between its entry and exit: n is 1 at every step and the label cache only
         // ever holds this volume's labels. The trapezoid half weights (project_kernel.cu:537) apply
         // to t = 0 and t = num_steps - 1 only, so those steps are peeled off the main loop.
@@ -497,7 +502,26 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
         // words as the reference's eager fetches, without fetching for volumes that do not count.
         int key_vol = -1;     // volume whose texture the cached word comes from
         bool key_ok = false;  // the word of (key_vol, key) has been fetched
+        int hidx[kMaxMeshLayers], hdepth[kMaxMeshLayers];
+#pragma unroll
+        for (int j = 0; j < kMaxMeshLayers; j++) hidx[j] = hdepth[j] = 0;
         for (; t < t_end; ++t) {
+            // subtractive meshes (project_kernel.cu:498-519): count the crossings before alpha
+            bool inside = false;
+            if (carve) {
+#pragma unroll
+                for (int j = 0; j < kMaxMeshLayers; j++) {
+                    if (j >= p.hit_layers) break;
+                    const size_t base = ((size_t)j * plane + pix) * p.max_hits;
+                    while (hidx[j] < p.max_hits) {
+                        const int f = p.hit_facing[base + hidx[j]];
+                        if (f == 0 || !(p.hit_alpha[base + hidx[j]] < alpha)) break;
+                        hdepth[j] += f;
+                        ++hidx[j];
+                    }
+                    inside |= hdepth[j] > 0;
+                }
+            }
             // priority resolution (project_kernel.cu:458-496) needs only alpha
             int cur = NV, n = 0;
 #pragma unroll
@@ -514,7 +538,7 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
             }
             float weight = 0.0f;
             if (n == 0) {
-                if (attenuate) store_ad<M>(ad, air, add_air(load_ad<M>(ad, air)));
+                if (attenuate && !inside) store_ad<M>(ad, air, add_air(load_ad<M>(ad, air)));
             } else {
                 weight = __fdiv_rn(1.0f, (float)n);
                 weight = __fmul_rn(weight, (0 == t || num_steps - 1 == t) ? 0.5f : 1.0f);
@@ -535,7 +559,7 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
                     key_ok = false;
                 }
                 // no range re-check, as in project_kernel.cu:541
-                if (n != 0 && trace[vol] && p.vol[vol].priority == cur) {
+                if (n != 0 && !inside && trace[vol] && p.vol[vol].priority == cur) {
                     if (!key_ok) {
 #pragma unroll
                         for (int i = 0; i < NV; i++)

@@ -20,6 +20,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <string>
 #include <vector>
 
 #include "../../include/drr_gb300.h"
@@ -43,9 +44,32 @@ constexpr double kMaxImageCoord = 1.0e6;
 
 __device__ __forceinline__ bool top_left(long long dx, long long dy) { return dy > 0 || (dy == 0 && dx < 0); }
 
+// Subtractive hit lists of one view: per layer and pixel up to max_hits (distance, facing) pairs,
+// facing +1 entering and -1 leaving, sorted by distance, facing 0 after the last hit.
+struct HitLists {
+    float *alpha;          // [n_layers][H][W][max_hits]
+    int8_t *facing;        // [n_layers][H][W][max_hits]
+    unsigned int *count;   // [n_layers][H][W] (building only)
+    int n_layers, max_hits;
+};
+
+enum { kModeAdditive = 1, kModeSubtractive = 2 };
+
+// density_between.frag: an additive crossing at distance d (sign +1 leaving, -1 entering) against the
+// subtractive pair [near, far] adds sign * rho * (far - max(d, near)) for d < far; summed over a
+// closed additive surface this removes rho times the overlap of its interior with [near, far].
+__device__ __forceinline__ double between(double d, double near, double far) {
+    if (d < near) return far - near;
+    if (d < far) return far - d;
+    return 0.0;
+}
+
+// pass 0: additive integrals (with subtraction by the hit lists of higher layers when given);
+// pass 1: append subtractive crossings to the hit lists
 __global__ void rasterize_kernel(const float *__restrict__ tri, const int32_t *__restrict__ slot,
-                                 const float *__restrict__ density, int n_tri, RasterView view, double *R, double *G,
-                                 int n_slots) {
+                                 const float *__restrict__ density, const int32_t *__restrict__ layer,
+                                 const uint8_t *__restrict__ mode, int n_tri, RasterView view, double *R, double *G,
+                                 int n_slots, HitLists hits, int pass) {
     const int lane = threadIdx.x & 31;
     const int warps_per_block = blockDim.x >> 5;
     const size_t plane = (size_t)view.width * view.height;
@@ -95,7 +119,10 @@ __global__ void rasterize_kernel(const float *__restrict__ tri, const int32_t *_
         const double np = n[0] * (P[0][0] - view.src[0]) + n[1] * (P[0][1] - view.src[1]) + n[2] * (P[0][2] - view.src[2]);
         const double rho = density[f];
         const int s = slot[f];
-        if (s < 0 || s >= n_slots) continue;
+        const int lay = layer ? layer[f] : 0;
+        const int md = mode ? mode[f] : kModeAdditive;
+        if (pass == 0 && (!(md & kModeAdditive) || s < 0 || s >= n_slots)) continue;
+        if (pass == 1 && (!(md & kModeSubtractive) || lay < 0 || lay >= hits.n_layers)) continue;
         const long long nu = u1 - u0 + 1, count = nu * (v1 - v0 + 1);
         for (long long idx = lane; idx < count; idx += 32) {
             const long long u = u0 + idx % nu, v = v0 + idx / nu;
@@ -116,9 +143,53 @@ __global__ void rasterize_kernel(const float *__restrict__ tri, const int32_t *_
             if (nr == 0.0) continue;  // ray in the triangle's plane
             const double dist = np / nr;
             const double sign = nr > 0.0 ? 1.0 : -1.0;
-            const size_t o = (size_t)s * plane + (size_t)v * view.width + (size_t)u;
-            atomicAdd(R + o, sign * dist * rho);
+            const size_t pix = (size_t)v * view.width + (size_t)u;
+            if (pass == 1) {
+                const size_t lp = (size_t)lay * plane + pix;
+                const unsigned int k = atomicAdd(hits.count + lp, 1u);
+                if ((int)k < hits.max_hits) {
+                    hits.alpha[lp * hits.max_hits + k] = (float)dist;
+                    hits.facing[lp * hits.max_hits + k] = sign > 0.0 ? (int8_t)-1 : (int8_t)1;
+                }
+                continue;
+            }
+            double r_add = sign * dist * rho;
+            for (int L = lay + 1; L < hits.n_layers; L++) {
+                const size_t base = ((size_t)L * plane + pix) * hits.max_hits;
+                for (int i = 0; i + 1 < hits.max_hits; i += 2) {
+                    if (hits.facing[base + i] == 0 || hits.facing[base + i + 1] == 0) break;
+                    r_add += sign * rho * between(dist, hits.alpha[base + i], hits.alpha[base + i + 1]);
+                }
+            }
+            const size_t o = (size_t)s * plane + pix;
+            atomicAdd(R + o, r_add);
             atomicAdd(G + o, sign);
+        }
+    }
+}
+
+// order each pixel's subtractive crossings by distance (insertion sort of at most max_hits) and
+// end the list with facing 0
+__global__ void sort_hits_kernel(HitLists hits, size_t n_lists) {
+    for (size_t l = (size_t)blockIdx.x * blockDim.x + threadIdx.x; l < n_lists; l += (size_t)gridDim.x * blockDim.x) {
+        float *a = hits.alpha + l * hits.max_hits;
+        int8_t *f = hits.facing + l * hits.max_hits;
+        const int n = min((int)hits.count[l], hits.max_hits);
+        for (int i = 1; i < n; i++) {
+            const float ai = a[i];
+            const int8_t fi = f[i];
+            int j = i - 1;
+            while (j >= 0 && a[j] > ai) {
+                a[j + 1] = a[j];
+                f[j + 1] = f[j];
+                --j;
+            }
+            a[j + 1] = ai;
+            f[j + 1] = fi;
+        }
+        for (int i = n; i < hits.max_hits; i++) {
+            a[i] = 0.0f;
+            f[i] = 0;
         }
     }
 }
@@ -150,17 +221,82 @@ bool invert3(const double *a, double *inv) {
 
 }  // namespace
 
+namespace {
+
+drr_status check_mesh(const drr_mesh_desc *mesh, const char *who) {
+    if (!mesh) return fail(DRR_ERR_INVALID_ARGUMENT, std::string(who) + ": NULL mesh");
+    if (mesh->n_slots < 1 || mesh->n_slots > DRR_MAX_MATERIALS)
+        return fail(DRR_ERR_INVALID_ARGUMENT, std::string(who) + ": n_slots outside [1, DRR_MAX_MATERIALS]");
+    if (mesh->n_triangles < 0 || (mesh->n_triangles > 0 && (!mesh->triangles || !mesh->slot || !mesh->density)))
+        return fail(DRR_ERR_INVALID_ARGUMENT, std::string(who) + ": bad triangle arrays");
+    if (mesh->n_layers < 0 || mesh->n_layers > DRR_MAX_MESH_LAYERS)
+        return fail(DRR_ERR_INVALID_ARGUMENT, std::string(who) + ": n_layers outside [0, DRR_MAX_MESH_LAYERS]");
+    return DRR_OK;
+}
+
+bool make_view(const double *world_from_index, const double *source_world, int v, int width, int height,
+               RasterView &rv) {
+    std::memcpy(rv.w, world_from_index + (size_t)v * 9, sizeof(rv.w));
+    std::memcpy(rv.src, source_world + (size_t)v * 3, sizeof(rv.src));
+    rv.width = width;
+    rv.height = height;
+    return invert3(rv.w, rv.winv);
+}
+
+int raster_blocks(int n_tri) { return (int)std::min<long long>(((long long)n_tri + 7) / 8, 65535LL * 4); }
+
+}  // namespace
+
+extern "C" drr_status drr_mesh_hits(const drr_mesh_desc *mesh, int32_t width, int32_t height,
+                                    const double *world_from_index, const double *source_world, int32_t max_hits,
+                                    float *hit_alpha, int8_t *hit_facing, void *stream) {
+    drr::set_last_error("");
+    drr_status st = check_mesh(mesh, "drr_mesh_hits");
+    if (st != DRR_OK) return st;
+    if (!world_from_index || !source_world || !hit_alpha || !hit_facing)
+        return fail(DRR_ERR_INVALID_ARGUMENT, "drr_mesh_hits: NULL argument");
+    if (width < 1 || height < 1) return fail(DRR_ERR_INVALID_ARGUMENT, "drr_mesh_hits: bad size");
+    if (max_hits < 2 || max_hits > 256 || (max_hits & 1))
+        return fail(DRR_ERR_INVALID_ARGUMENT, "drr_mesh_hits: max_hits must be even, in [2, 256]");
+    if (mesh->n_layers < 1) return DRR_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t plane = (size_t)width * height, lists = plane * mesh->n_layers;
+    RasterView rv;
+    if (!make_view(world_from_index, source_world, 0, width, height, rv))
+        return fail(DRR_ERR_INVALID_ARGUMENT, "drr_mesh_hits: singular world_from_index");
+    HitLists h{hit_alpha, hit_facing, nullptr, mesh->n_layers, max_hits};
+    cudaError_t e = cudaMallocAsync((void **)&h.count, lists * sizeof(unsigned int), s);
+    if (e != cudaSuccess) return cuda_fail(e, "drr_mesh_hits: scratch");
+    e = cudaMemsetAsync(h.count, 0, lists * sizeof(unsigned int), s);
+    if (e == cudaSuccess && mesh->n_triangles > 0) {
+        rasterize_kernel<<<raster_blocks(mesh->n_triangles), 256, 0, s>>>(
+            mesh->triangles, mesh->slot, mesh->density, mesh->layer, mesh->mode, mesh->n_triangles, rv, nullptr,
+            nullptr, mesh->n_slots, h, 1);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) {
+        const size_t nb = (lists + 255) / 256;
+        sort_hits_kernel<<<(unsigned)(nb < 4864 ? nb : 4864), 256, 0, s>>>(h, lists);
+        e = cudaGetLastError();
+    }
+    cudaFreeAsync(h.count, s);
+    if (e != cudaSuccess) return cuda_fail(e, "drr_mesh_hits");
+    return DRR_OK;
+}
+
 extern "C" drr_status drr_mesh_area_density(const drr_mesh_desc *mesh, int32_t width, int32_t height,
                                             int32_t n_views, const double *world_from_index,
-                                            const double *source_world, float *out, void *stream) {
+                                            const double *source_world, const float *hit_alpha,
+                                            const int8_t *hit_facing, int32_t max_hits, float *out, void *stream) {
     drr::set_last_error("");
-    if (!mesh || !world_from_index || !source_world || !out)
+    drr_status st = check_mesh(mesh, "drr_mesh_area_density");
+    if (st != DRR_OK) return st;
+    if (!world_from_index || !source_world || !out)
         return fail(DRR_ERR_INVALID_ARGUMENT, "drr_mesh_area_density: NULL argument");
     if (width < 1 || height < 1 || n_views < 0) return fail(DRR_ERR_INVALID_ARGUMENT, "drr_mesh_area_density: bad size");
-    if (mesh->n_slots < 1 || mesh->n_slots > DRR_MAX_MATERIALS)
-        return fail(DRR_ERR_INVALID_ARGUMENT, "drr_mesh_area_density: n_slots outside [1, DRR_MAX_MATERIALS]");
-    if (mesh->n_triangles < 0 || (mesh->n_triangles > 0 && (!mesh->triangles || !mesh->slot || !mesh->density)))
-        return fail(DRR_ERR_INVALID_ARGUMENT, "drr_mesh_area_density: bad triangle arrays");
+    if (hit_alpha && (n_views != 1 || !hit_facing || max_hits < 2 || (max_hits & 1)))
+        return fail(DRR_ERR_INVALID_ARGUMENT,
+                    "drr_mesh_area_density: hit lists need one view, facings and an even max_hits >= 2");
     cudaStream_t s = (cudaStream_t)stream;
     const size_t plane = (size_t)width * height, per_view = plane * mesh->n_slots;
     if (n_views == 0) return DRR_OK;
@@ -168,21 +304,19 @@ extern "C" drr_status drr_mesh_area_density(const drr_mesh_desc *mesh, int32_t w
     cudaError_t e = cudaMallocAsync((void **)&R, 2 * per_view * sizeof(double), s);
     if (e != cudaSuccess) return cuda_fail(e, "drr_mesh_area_density: scratch");
     double *G = R + per_view;
+    HitLists h{const_cast<float *>(hit_alpha), const_cast<int8_t *>(hit_facing), nullptr,
+               hit_alpha ? mesh->n_layers : 0, hit_alpha ? max_hits : 0};
     for (int v = 0; v < n_views && e == cudaSuccess; v++) {
         RasterView rv;
-        std::memcpy(rv.w, world_from_index + (size_t)v * 9, sizeof(rv.w));
-        std::memcpy(rv.src, source_world + (size_t)v * 3, sizeof(rv.src));
-        rv.width = width;
-        rv.height = height;
-        if (!invert3(rv.w, rv.winv)) {
+        if (!make_view(world_from_index, source_world, v, width, height, rv)) {
             cudaFreeAsync(R, s);
             return fail(DRR_ERR_INVALID_ARGUMENT, "drr_mesh_area_density: singular world_from_index");
         }
         e = cudaMemsetAsync(R, 0, 2 * per_view * sizeof(double), s);
         if (e == cudaSuccess && mesh->n_triangles > 0) {
-            const int blocks = (int)std::min<long long>(((long long)mesh->n_triangles + 7) / 8, 65535LL * 4);
-            rasterize_kernel<<<blocks, 256, 0, s>>>(mesh->triangles, mesh->slot, mesh->density, mesh->n_triangles, rv,
-                                                    R, G, mesh->n_slots);
+            rasterize_kernel<<<raster_blocks(mesh->n_triangles), 256, 0, s>>>(
+                mesh->triangles, mesh->slot, mesh->density, mesh->layer, mesh->mode, mesh->n_triangles, rv, R, G,
+                mesh->n_slots, h, 0);
             e = cudaGetLastError();
         }
         if (e == cudaSuccess) {

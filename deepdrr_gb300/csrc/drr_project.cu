@@ -96,6 +96,10 @@ void fill_scene(drr::SceneParams<NV> &p, const drr_volset *set, const drr_tables
     p.mesh_ad = a.mesh_area_density;
     p.n_mesh = a.mesh_area_density ? a.n_mesh_slots : 0;
     for (int k = 0; k < p.n_mesh && k < drr::kMaxMeshSlots; k++) p.mesh_mat[k] = a.mesh_material[k];
+    p.hit_alpha = a.mesh_hit_alpha;
+    p.hit_facing = a.mesh_hit_facing;
+    p.hit_layers = a.mesh_hit_alpha ? a.mesh_hit_layers : 0;
+    p.max_hits = a.mesh_hit_alpha ? a.max_mesh_hits : 0;
 }
 
 template <int NV>
@@ -249,6 +253,12 @@ drr_status validate(const drr_volset *set, const drr_tables *tables, const drr_p
             return fail(DRR_ERR_INVALID_ARGUMENT, "drr_project: priority outside [0, n_volumes)");
     if ((a.flags & DRR_FLAG_ATTENUATE_OUTSIDE) && (a.air_index < 0 || a.air_index >= set->n_materials))
         return fail(DRR_ERR_INVALID_ARGUMENT, "drr_project: air_index outside [0, n_materials)");
+    if (a.mesh_hit_alpha) {
+        if (!a.mesh_hit_facing || a.mesh_hit_layers < 1 || a.mesh_hit_layers > drr::kMaxMeshLayers ||
+            a.max_mesh_hits < 2 || a.n_views > 1)
+            return fail(DRR_ERR_INVALID_ARGUMENT,
+                        "drr_project: subtractive hit lists need facings, 1-4 layers, max_mesh_hits >= 2 and one view");
+    }
     if (a.mesh_area_density) {
         if (a.n_mesh_slots < 1 || a.n_mesh_slots > drr::kMaxMeshSlots || !a.mesh_material)
             return fail(DRR_ERR_INVALID_ARGUMENT, "drr_project: mesh slots outside [1, 16] or no slot materials");

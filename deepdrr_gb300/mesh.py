@@ -5,8 +5,9 @@ with deepdrr/pyrenderdrr/material.py): triangles with a pose, a material name an
 (g/cm^3; defaults from the reference's DRRMaterial table), and whether the mesh is additive. The
 reference renders meshes with OpenGL; this package rasterises them in CUDA (drr_mesh_area_density).
 
-Subtractive meshes (material.subtractive, which carve the volumes and lower mesh layers) are not
-supported: constructing one raises NotImplementedError.
+A subtractive mesh (``subtractive=True``) removes, along each ray, the volumes' samples inside it
+and the parts of additive meshes of lower layers inside it (the reference's MESH_SUB pass); an
+additive one adds its material's path length. A mesh can be both, as a reference material can.
 """
 from __future__ import annotations
 
@@ -55,9 +56,14 @@ class Mesh:
 
     def __init__(self, vertices: np.ndarray, faces: np.ndarray, material: str = "iron",
                  density: Optional[float] = None, additive: bool = True, subtractive: bool = False,
-                 world_from_anatomical: Optional[FrameTransform] = None, enabled: bool = True):
-        if subtractive or not additive:
-            raise NotImplementedError("only additive meshes are supported")
+                 layer: int = 0, world_from_anatomical: Optional[FrameTransform] = None, enabled: bool = True):
+        if not (additive or subtractive):
+            raise ValueError("a mesh must be additive, subtractive or both")
+        self.additive = bool(additive)
+        self.subtractive = bool(subtractive)
+        self.layer = int(layer)
+        if self.layer < 0:
+            raise ValueError("layer must be >= 0")
         self.vertices = np.asarray(vertices, dtype=np.float64).reshape(-1, 3)
         self.faces = np.asarray(faces, dtype=np.int64).reshape(-1, 3)
         if self.faces.size and (self.faces.min() < 0 or self.faces.max() >= len(self.vertices)):

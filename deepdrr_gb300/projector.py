@@ -367,49 +367,75 @@ class Projector:
         self.output_shape = (W0, H0)
         return a, out
 
+    @property
+    def _has_subtractive(self) -> bool:
+        return any(m.subtractive and m.enabled for m in self.meshes)
+
     def _mesh_args(self, a, wfi, src, width, height, keep, stream=None) -> None:
-        """Rasterise the enabled additive meshes for the views of `a` (drr_mesh_area_density) and
-        point `a` at the result."""
+        """Rasterise the enabled meshes for the views of `a` and point `a` at the results: additive
+        integrals (drr_mesh_area_density) and, with subtractive meshes (one view per call), the
+        subtractive hit lists (drr_mesh_hits) the march and the additive pass consult."""
         import torch
 
         n = wfi.shape[0]
         S = len(self.mesh_materials)
         out = torch.empty((n, S, height, width), dtype=torch.float32, device=self.torch_device)
-        tris, slot, dens = self._mesh_triangles()
-        self._mesh_fill(tris, slot, dens, wfi, src, width, height, out, keep, stream)
+        desc = self._mesh_desc(keep)
+        hits = None
+        if self._has_subtractive:
+            if n != 1:
+                raise ValueError("subtractive meshes are rendered one view per call")
+            L, K = self.mesh_layers, self.max_mesh_hits
+            ha = torch.empty((L, height, width, K), dtype=torch.float32, device=self.torch_device)
+            hf = torch.empty((L, height, width, K), dtype=torch.int8, device=self.torch_device)
+            _lib.check(_lib.load().drr_mesh_hits(ctypes.byref(desc), width, height, wfi.ctypes.data, src.ctypes.data,
+                                                 K, ha.data_ptr(), hf.data_ptr(), self._stream_ptr(stream)))
+            keep += [ha, hf]
+            hits = (ha, hf)
+            a.mesh_hit_alpha = ha.data_ptr()
+            a.mesh_hit_facing = hf.data_ptr()
+            a.mesh_hit_layers = L
+            a.max_mesh_hits = K
+        self._mesh_fill(desc, wfi, src, width, height, out, hits, stream)
         mats = np.asarray([self.all_materials.index(m) for m in self.mesh_materials], dtype=np.int32)
         keep += [out, mats]
         a.mesh_area_density = out.data_ptr()
         a.n_mesh_slots = S
         a.mesh_material = mats.ctypes.data
 
-    def _mesh_triangles(self):
-        """(triangles [F, 9] float32 world, slot [F] int32, density [F] float32) of the enabled meshes."""
+    def _mesh_desc(self, keep):
+        """drr_mesh_desc of the enabled meshes (world-space triangles, slots, densities, layers, modes)."""
+        import torch
+
         meshes = [m for m in self.meshes if m.enabled and len(m.faces)]
+        desc = _lib.drr_mesh_desc()
+        desc.n_slots = len(self.mesh_materials)
+        desc.n_layers = self.mesh_layers if self._has_subtractive else 0
         if not meshes:
-            return np.zeros((0, 9), np.float32), np.zeros(0, np.int32), np.zeros(0, np.float32)
+            desc.n_triangles = 0
+            return desc
+        for m in meshes:
+            if m.subtractive and m.layer >= self.mesh_layers:
+                raise ValueError(f"mesh layer {m.layer} >= mesh_layers ({self.mesh_layers})")
         tris = np.concatenate([m.triangles_in_world().reshape(-1, 9) for m in meshes]).astype(np.float32)
         slot = np.concatenate([np.full(len(m.faces), self.mesh_materials.index(m.material), np.int32) for m in meshes])
         dens = np.concatenate([np.full(len(m.faces), m.density, np.float32) for m in meshes])
-        return tris, slot, dens
-
-    def _mesh_fill(self, tris, slot, dens, wfi, src, width, height, out, keep, stream=None) -> None:
-        import torch
-
-        dev = self.torch_device
-        t_tris = torch.from_numpy(np.ascontiguousarray(tris)).to(dev)
-        t_slot = torch.from_numpy(np.ascontiguousarray(slot)).to(dev)
-        t_dens = torch.from_numpy(np.ascontiguousarray(dens)).to(dev)
-        desc = _lib.drr_mesh_desc()
-        desc.triangles = t_tris.data_ptr() if len(tris) else None
-        desc.slot = t_slot.data_ptr() if len(tris) else None
-        desc.density = t_dens.data_ptr() if len(tris) else None
+        layer = np.concatenate([np.full(len(m.faces), m.layer, np.int32) for m in meshes])
+        mode = np.concatenate([np.full(len(m.faces), (_lib.DRR_MESH_ADDITIVE if m.additive else 0)
+                                       | (_lib.DRR_MESH_SUBTRACTIVE if m.subtractive else 0), np.uint8)
+                               for m in meshes])
+        t = [torch.from_numpy(np.ascontiguousarray(x)).to(self.torch_device) for x in (tris, slot, dens, layer, mode)]
+        keep += t
+        desc.triangles, desc.slot, desc.density, desc.layer, desc.mode = (x.data_ptr() for x in t)
         desc.n_triangles = len(tris)
-        desc.n_slots = len(self.mesh_materials)
-        _lib.check(_lib.load().drr_mesh_area_density(ctypes.byref(desc), width, height, wfi.shape[0],
-                                                     wfi.ctypes.data, src.ctypes.data, out.data_ptr(),
-                                                     self._stream_ptr(stream)))
-        keep += [t_tris, t_slot, t_dens]
+        return desc
+
+    def _mesh_fill(self, desc, wfi, src, width, height, out, hits=None, stream=None) -> None:
+        ha, hf = hits if hits is not None else (None, None)
+        _lib.check(_lib.load().drr_mesh_area_density(
+            ctypes.byref(desc), width, height, wfi.shape[0], wfi.ctypes.data, src.ctypes.data,
+            ha.data_ptr() if ha is not None else None, hf.data_ptr() if hf is not None else None,
+            self.max_mesh_hits if ha is not None else 0, out.data_ptr(), self._stream_ptr(stream)))
 
     def _stream_ptr(self, stream):
         import torch
@@ -429,6 +455,13 @@ class Projector:
         ``solid_angle`` [N, H, W]. ``ijk_from_world`` ([n_volumes][3][4], float64) replaces the
         volumes' poses for this call."""
         camera_projections = self._prepare_project(camera_projections)
+        if self._has_subtractive and len(camera_projections) > 1:
+            # subtractive hit lists are built per view (projector.py:709-716 renders meshes per view)
+            import torch
+
+            parts = [self.project_tensors(p, area_density=area_density, solid_angle=solid_angle, flags=flags,
+                                          stream=stream, ijk_from_world=ijk_from_world) for p in camera_projections]
+            return {k: torch.cat([q[k] for q in parts]) for k in parts[0]}
         keep = []
         a, out = self._args(camera_projections, area_density, solid_angle,
                             flags | (_lib.DRR_FLAG_PERSISTENT if persistent else 0), launch, keep, ijk_from_world)
@@ -609,6 +642,8 @@ class ProjectionGraph:
     """
 
     def __init__(self, projector: Projector, camera_projections, area_density: bool, launch: Optional[dict]):
+        if projector._has_subtractive:
+            raise NotImplementedError("subtractive meshes are rendered one view per call, not in a graph")
         self.projector = projector
         self._keep = []
         self.args, self.outputs = projector._args(camera_projections, area_density, False,
@@ -632,8 +667,7 @@ class ProjectionGraph:
         if self.projector.meshes:
             # the graph reads the mesh integrals from a fixed buffer: rasterise the new views into it
             out = self.outputs["_mesh_area_density"]
-            tris, slot, dens = self.projector._mesh_triangles()
-            self.projector._mesh_fill(tris, slot, dens, wfi, src, W0, H0, out, self._keep)
+            self.projector._mesh_fill(self.projector._mesh_desc(self._keep), wfi, src, W0, H0, out)
         _lib.check(_lib.load().drr_graph_set_views(self._graph, wfi.ctypes.data, src.ctypes.data, ijk.ctypes.data))
 
     def launch(self, stream=None) -> dict:

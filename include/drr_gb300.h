@@ -16,6 +16,7 @@
  *                       launch, projector.py:709-800, 802-831; kernel deepdrr/projector/project_kernel.cu:135-650
  *   drr_*_destroy       Projector.free, projector.py:1719-1764
  *   drr_ingest_hu       Volume.from_hu's HU conversion and thresholding, deepdrr/vol/volume.py:281-351
+ *   drr_mesh_*          the reference's OpenGL mesh passes (pyrenderdrr) read by project_kernel.cu
  *   drr_add_noise       analytic_generators.add_noise, deepdrr/projector/analytic_generators.py:10-18
  *   drr_clip_upper,     the post-processing of Projector.project, projector.py:697-702, and
  *   drr_neglog          deepdrr/utils/image_utils.py:18-58
@@ -142,27 +143,55 @@ typedef struct {
     const float *mesh_area_density; /* device [n_views][n_mesh_slots][H][W], mm g/cm^3 */
     int32_t n_mesh_slots;
     const int32_t *mesh_material;   /* host [n_mesh_slots]: material index of each slot */
+    /* subtractive meshes (drr_mesh_hits, n_views must be 1): samples inside any layer's surfaces add
+       nothing, neither volume nor air (project_kernel.cu:498-521); NULL for none */
+    const float *mesh_hit_alpha;    /* device [mesh_hit_layers][H][W][max_mesh_hits] */
+    const int8_t *mesh_hit_facing;  /* device, same shape */
+    int32_t mesh_hit_layers;
+    int32_t max_mesh_hits;
 } drr_project_args;
 
-/* Triangles of the additive meshes of a projector. */
+#define DRR_MAX_MESH_LAYERS 4
+
+enum { DRR_MESH_ADDITIVE = 1, DRR_MESH_SUBTRACTIVE = 2 };
+
+/* Triangles of the meshes of a projector. */
 typedef struct {
     const float *triangles; /* device [n_triangles][3][3]: vertices in world coordinates (mm), wound so the
                                right-handed normal points out of the closed surface */
     const int32_t *slot;    /* device [n_triangles]: mesh-material slot in [0, n_slots) */
     const float *density;   /* device [n_triangles]: density of the triangle's mesh (g/cm^3) */
+    const int32_t *layer;   /* device [n_triangles]: mesh layer in [0, n_layers), or NULL for all 0 */
+    const uint8_t *mode;    /* device [n_triangles]: DRR_MESH_ADDITIVE | DRR_MESH_SUBTRACTIVE bits, or NULL
+                               for all additive */
     int32_t n_triangles;
     int32_t n_slots;
+    int32_t n_layers;       /* layers of the subtractive hit lists, [0, DRR_MAX_MESH_LAYERS] */
 } drr_mesh_desc;
+
+/* Subtractive hit lists of ONE view (the view's ray matrix and source as in drr_project_args): per
+ * layer and pixel the distances along the pixel's centre ray at which it crosses the layer's
+ * subtractive surfaces, sorted, with facing +1 entering and -1 leaving and 0 after the last (at most
+ * max_hits, even, kept; further crossings are dropped). hit_alpha / hit_facing are device
+ * [n_layers][H][W][max_hits]. Replaces the reference's depth-peeled hit textures and their clean-up
+ * (projector.py:1124-1256, peel_postprocess_kernel.cu:15-235). */
+drr_status drr_mesh_hits(const drr_mesh_desc *mesh, int32_t width, int32_t height, const double *world_from_index,
+                         const double *source_world, int32_t max_hits, float *hit_alpha, int8_t *hit_facing,
+                         void *stream);
 
 /* Path integrals of additive meshes through every pixel of `n_views` views (the views' ray matrices
  * and sources as in drr_project_args), into `out` (device [n_views][n_slots][H][W], mm g/cm^3):
  * per slot max(sum of signed distance x density over the surfaces the pixel's centre ray crosses, 0)
- * where the crossings balance, else 0. Replaces the reference's OpenGL density pass
- * (pyrenderdrr/renderer.py, shaders/density.frag:9-13) and its read-back (projector.py:1063-1088,
- * 1302-1330); rasterised in CUDA with 1/256-pixel snapping and a top-left rule, so shared edges
- * count once. Triangles reaching behind the source are not rasterised. */
+ * where the crossings balance, else 0. With subtractive hit lists (one view only), the parts of a
+ * layer-l additive mesh inside the consecutive hit pairs of every layer above l are removed, as the
+ * reference's density_between pass does (shaders/density_between.frag, projector.py:1258-1300).
+ * Replaces the reference's OpenGL density pass (pyrenderdrr/renderer.py, shaders/density.frag:9-13)
+ * and its read-back (projector.py:1063-1088, 1302-1330); rasterised in CUDA with 1/256-pixel snapping
+ * and a top-left rule, so shared edges count once. Triangles reaching behind the source are not
+ * rasterised. */
 drr_status drr_mesh_area_density(const drr_mesh_desc *mesh, int32_t width, int32_t height, int32_t n_views,
-                                 const double *world_from_index, const double *source_world, float *out,
+                                 const double *world_from_index, const double *source_world,
+                                 const float *hit_alpha, const int8_t *hit_facing, int32_t max_hits, float *out,
                                  void *stream);
 
 /* Render `args->n_views` views into the caller's device buffers, asynchronously on `stream`.

@@ -16,15 +16,9 @@ from __future__ import annotations
 import numpy as np
 
 
-def mesh_area_density(triangles: np.ndarray, slot: np.ndarray, density: np.ndarray, n_slots: int,
-                      world_from_index: np.ndarray, source: np.ndarray, width: int, height: int) -> np.ndarray:
-    """[n_slots, H, W] float32 additive path integrals (mm g/cm^3) of one view."""
-    W = np.asarray(world_from_index, dtype=np.float64).reshape(3, 3)
-    Winv = np.linalg.inv(W)
-    s = np.asarray(source, dtype=np.float64).reshape(3)
-    R = np.zeros((n_slots, height, width))
-    G = np.zeros((n_slots, height, width))
-    tri = np.asarray(triangles, dtype=np.float32).astype(np.float64).reshape(-1, 3, 3)
+def _crossings(tri, W, Winv, s, width, height):
+    """(triangle, u, v, distance, sign) arrays for each triangle that covers some pixel centre."""
+    out = []
     for f in range(tri.shape[0]):
         P = tri[f]
         q = (P - s) @ Winv.T
@@ -64,10 +58,65 @@ def mesh_area_density(triangles: np.ndarray, slot: np.ndarray, density: np.ndarr
         r = np.stack([fu, fv, np.ones_like(fu)], 1) @ W.T
         nr = (r @ n) / np.linalg.norm(r, axis=1)
         ok = nr != 0
-        dist = npd / nr[ok]
-        sign = np.where(nr[ok] > 0, 1.0, -1.0)
-        iv, iu = vv[cov][ok], uu[cov][ok]
-        np.add.at(R[int(slot[f])], (iv, iu), sign * dist * float(density[f]))
-        np.add.at(G[int(slot[f])], (iv, iu), sign)
+        out.append((f, uu[cov][ok], vv[cov][ok], npd / nr[ok], np.where(nr[ok] > 0, 1.0, -1.0)))
+    return out
+
+
+def _view(world_from_index, source, triangles):
+    W = np.asarray(world_from_index, dtype=np.float64).reshape(3, 3)
+    return (W, np.linalg.inv(W), np.asarray(source, dtype=np.float64).reshape(3),
+            np.asarray(triangles, dtype=np.float32).astype(np.float64).reshape(-1, 3, 3))
+
+
+def hit_lists(triangles, layer, mode, n_layers: int, max_hits: int, world_from_index, source, width: int,
+              height: int):
+    """Subtractive crossings of one view: (alpha [L, H, W, K] float32, facing int8), sorted by
+    distance, facing +1 entering and -1 leaving, 0 after the last (at most max_hits kept)."""
+    W, Winv, s, tri = _view(world_from_index, source, triangles)
+    lists = [[[[] for _ in range(width)] for _ in range(height)] for _ in range(n_layers)]
+    for f, uu, vv, dist, sign in _crossings(tri, W, Winv, s, width, height):
+        if not (int(mode[f]) & 2) or not (0 <= int(layer[f]) < n_layers):
+            continue
+        for u, v, d, g in zip(uu, vv, dist, sign):
+            lists[int(layer[f])][v][u].append((np.float32(d), -1 if g > 0 else 1))
+    A = np.zeros((n_layers, height, width, max_hits), np.float32)
+    F = np.zeros((n_layers, height, width, max_hits), np.int8)
+    for L in range(n_layers):
+        for v in range(height):
+            for u in range(width):
+                h = sorted(lists[L][v][u], key=lambda x: x[0])[:max_hits]
+                for k, (d, g) in enumerate(h):
+                    A[L, v, u, k], F[L, v, u, k] = d, g
+    return A, F
+
+
+def mesh_area_density(triangles: np.ndarray, slot: np.ndarray, density: np.ndarray, n_slots: int,
+                      world_from_index: np.ndarray, source: np.ndarray, width: int, height: int,
+                      layer=None, mode=None, hits=None) -> np.ndarray:
+    """[n_slots, H, W] float32 additive path integrals (mm g/cm^3) of one view. With `hits` (from
+    hit_lists) the parts of a layer-l additive mesh inside the consecutive hit pairs of every layer
+    above l are removed (density_between.frag)."""
+    W, Winv, s, tri = _view(world_from_index, source, triangles)
+    R = np.zeros((n_slots, height, width))
+    G = np.zeros((n_slots, height, width))
+    nF = tri.shape[0]
+    layer = np.zeros(nF, np.int64) if layer is None else np.asarray(layer)
+    mode = np.ones(nF, np.int64) if mode is None else np.asarray(mode)
+    for f, uu, vv, dist, sign in _crossings(tri, W, Winv, s, width, height):
+        if not (int(mode[f]) & 1):
+            continue
+        rho = float(density[f])
+        add = sign * dist * rho
+        if hits is not None:
+            A, F = hits
+            for L in range(int(layer[f]) + 1, A.shape[0]):
+                for i in range(0, A.shape[3] - 1, 2):
+                    pair_ok = (F[L, vv, uu, i] != 0) & (F[L, vv, uu, i + 1] != 0)
+                    near = A[L, vv, uu, i].astype(np.float64)
+                    far = A[L, vv, uu, i + 1].astype(np.float64)
+                    g = np.where(dist < near, far - near, np.where(dist < far, far - dist, 0.0))
+                    add = add + np.where(pair_ok, sign * rho * g, 0.0)
+        np.add.at(R[int(slot[f])], (vv, uu), add)
+        np.add.at(G[int(slot[f])], (vv, uu), sign)
     Rf, Gf = R.astype(np.float32), G.astype(np.float32)
     return np.where(np.abs(Gf) < 0.00001, np.maximum(Rf, 0.0), 0.0).astype(np.float32)

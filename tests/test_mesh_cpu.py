@@ -45,9 +45,11 @@ def test_stl_round_trip(tmp_path):
     assert m2.density == DEFAULT_DENSITIES["titanium"] and len(m2.faces) == len(tri)
 
 
-def test_mesh_rejects_subtractive_and_unknown_density():
-    with pytest.raises(NotImplementedError):
-        Mesh.box(subtractive=True)
+def test_mesh_flags_and_unknown_density():
+    m = Mesh.box(subtractive=True, additive=False, layer=1)
+    assert m.subtractive and not m.additive and m.layer == 1
+    with pytest.raises(ValueError):
+        Mesh.box(additive=False, subtractive=False)
     with pytest.raises(ValueError):
         Mesh.box(material="unobtainium")
 
