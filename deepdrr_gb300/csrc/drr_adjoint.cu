@@ -6,12 +6,7 @@ namespace drr {
 template <int M>
 cudaError_t launch_adjoint(const AdjointParams &p, cudaStream_t stream) {
     const dim3 grid((p.s.width + kTileW - 1) / kTileW, (p.s.height + kTileH - 1) / kTileH, p.n_views);
-    if (p.grad_density != nullptr) {
-        adjoint_density_kernel<M><<<grid, kBlockThreads, 0, stream>>>(p);
-        cudaError_t e = cudaGetLastError();
-        if (e != cudaSuccess) return e;
-    }
-    if (p.grad_pose != nullptr) adjoint_pose_kernel<M><<<grid, kBlockThreads, 0, stream>>>(p);
+    adjoint_kernel<M><<<grid, kBlockThreads, 0, stream>>>(p);
     return cudaGetLastError();
 }
 

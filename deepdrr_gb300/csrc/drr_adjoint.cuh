@@ -5,26 +5,34 @@
 //
 //   * dL/d(density): the exact adjoint of forward_kernel. A sample at p adds w_t * rho(p) * seg_m(p)
 //     to the raw path length of material m, with rho(p) = sum_c W_c rho_c over the texture unit's
-//     8-bit corner weights W_c at coordinate p + 0.5 (the staged rule the oracle's
-//     hw_corner_weights states). So dL/d(rho_c) = sum over samples of w_t W_c sum_m gr_m seg_m,
-//     gr_m = dL/d(raw path length m). Contributions are summed per ray in registers while the
-//     sample stays in the same texel cell and added to the gradient volume when it leaves it
-//     (adjoint_density_kernel).
+//     8-bit corner weights W_c at coordinate p + 0.5 (drr_texweights.h). So dL/d(rho_c) = sum over
+//     samples of w_t W_c q_t, q_t = sum_m gr_m seg_m(p_t) and gr_m = dL/d(raw path length m).
 //   * dL/d(pose): the derivative of a rigid motion of the volume, theta = (translation t,
 //     rotation vector w about `center`, world frame), at theta = 0. Because the filtered density is
 //     piecewise constant in p (8-bit weights), the position derivative uses the continuous
 //     trilinear interpolation of the same texels and labels: h = w_t (grad rho Q + rho grad Q) with
 //     Q the trilinear interpolation of gr over the eight corner labels. With q = A^T h (A the 3x3 of
 //     IJK_from_world) and x_t = source + alpha_t r: dL/dt = -sum q, dL/dw = -sum (x_t - center) x q.
-//     Changes of the step count and of the entry / exit samples with the pose are not differentiated
-//     (adjoint_pose_kernel).
+//     Changes of the step count and of the entry / exit samples with the pose are not differentiated.
 //
-// The march reproduces the forward's samples exactly (same float32 alpha sequence, same live step
-// range, same trapezoid half weights). Only single-volume projections without air attenuation
-// outside the volume are differentiated.
+// One kernel computes both. Each thread marches one ray over exactly the forward's samples (same
+// float32 alpha sequence, same live step range, same trapezoid half weights); the 32 rays of a warp
+// step together. A ray's samples fall into runs: a density run is a stretch of samples in one
+// texture-filter cell with one value of w_t q_t, a pose run a stretch in one label cell with one
+// trapezoid weight. Within a run the per-sample work is small and identical across the warp: the
+// eight integer corner weights are summed two to a register (drr_texweights.h), and a pose run only
+// counts its samples. When a run ends, the ray appends it to a per-warp queue in shared memory; the
+// warp drains the queues together once they are half full, so the per-cell work -- eight texel
+// additions to the gradient volume per density run, eight texel fetches and the gradient sums per
+// pose run -- runs with all lanes busy instead of once per lane that happens to change cell.
+// A pose run in a cell whose eight labels agree is summed in closed form: Q is constant there and
+// grad rho is bilinear in the fractions, so its sums over the run's evenly spaced samples are
+// polynomials in the run length; runs in mixed cells are evaluated sample by sample in the drain.
+// Only single-volume projections without air attenuation outside the volume are differentiated.
 #pragma once
 
 #include "drr_forward.cuh"
+#include "drr_texweights.h"
 
 namespace drr {
 
@@ -48,45 +56,6 @@ struct AdjointParams {
     float center[3];                    // rotation centre, world
 };
 
-// Corner weights of the texture unit for the density coordinate x = p + 0.5 on one axis of n
-// texels: texel i0 = fix >> 8, fraction a = fix & 255 (see the oracle's tex_linear). v = 256 x - 128
-// is exact wherever it is >= 0 (256 x is exact and 128 a multiple of its ulp, so the fused form
-// rounds nothing there); after the unit's own clamp to [0, (n - 1) 256], v is a multiple of 2^-16
-// below 2^17, so v + 0.5 is exact and rounding half up is one round-down conversion.
-__device__ __forceinline__ void hw_axis(float x, int n, int &i0, int &i1, int &a) {
-    float v = __fmaf_rn(x, 256.0f, -128.0f);
-    v = fminf(fmaxf(v, 0.0f), (float)(n - 1) * 256.0f);
-    const int fix = __float2int_rd(__fadd_rn(v, 0.5f));
-    i0 = fix >> 8;
-    a = fix & 255;
-    i1 = min(i0 + 1, n - 1);
-}
-
-__device__ __forceinline__ void hw_weights(int Ax, int Ay, int Az, int W[8]) {
-#pragma unroll
-    for (int dz = 0; dz <= 1; dz++) {
-        const int vz = dz ? Az : 256 - Az;
-        const int hx = (vz * Ax + 128) >> 8;
-#pragma unroll
-        for (int dx = 0; dx <= 1; dx++) {
-            const int vx = dx ? hx : vz - hx;
-            const int hy = dx ? (vx * Ay + 128) >> 8 : vx - ((vx * (256 - Ay) + 128) >> 8);
-            W[dx | 2 | (dz << 2)] = hy;
-            W[dx | (dz << 2)] = vx - hy;
-        }
-    }
-}
-
-// Material weight of label L: gr[L].
-template <int M>
-__device__ __forceinline__ float gr_of(const float gr[M], int L) {
-    float v = 0.0f;
-#pragma unroll
-    for (int m = 0; m < M; m++)
-        if (m == L) v = gr[m];
-    return v;
-}
-
 // Trilinear gradient of eight corner values c = dx | dy << 1 | dz << 2 at fractions (fx, fy, fz).
 __device__ __forceinline__ void trilinear_grad(const float v[8], float fx, float fy, float fz, float gx, float gy,
                                                float gz, float d[3]) {
@@ -101,7 +70,7 @@ __device__ __forceinline__ float trilinear(const float v[8], float fx, float fy,
            fz * (gy * (gx * v[4] + fx * v[5]) + fy * (gx * v[6] + fx * v[7]));
 }
 
-// Per-ray state of both adjoint kernels: the upstream material weights and the forward's march.
+// Per-ray state of the adjoint: the upstream material weights and the forward's march.
 template <int M>
 struct AdjointRay {
     float gr[M];  // dL/d(raw path length of material m), i.e. dL/d(area density) * step / 10
@@ -198,251 +167,380 @@ __device__ __forceinline__ bool adjoint_setup(const AdjointParams &P, const Adjo
     return R.t < R.t_end;
 }
 
-// Density gradient: the exact transpose of the forward's samples. Each sample adds
-// w_t q_t W_c / 256 to texel c of its hardware-filter cell (q_t = sum_m gr_m seg_m). While the cell
-// and w_t q_t stay the same the integer weights W_c are summed and converted once; the cell's eight
-// sums are added to the gradient volume when the ray leaves it.
+// Per-warp run queue of adjoint_kernel: a ring of kAdjQueue entries (structure of arrays, word k
+// of entry e at [k][e]); the warp drains 32 runs at a time.
+constexpr int kAdjQueue = 64;
+constexpr int kRunWords = 7;  // alpha0, count | lane << 8 | half << 13, label word, four packed corner sums
+constexpr int kMixWords = 3;  // alpha, lane << 8 | half << 13, label word
+
 template <int M>
-__global__ void __launch_bounds__(kBlockThreads) adjoint_density_kernel(const __grid_constant__ AdjointParams P) {
+struct AdjointWarpSmem {
+    uint32_t run[kRunWords][kAdjQueue];  // runs in cells whose eight labels agree
+    uint32_t mix[kMixWords][kAdjQueue];  // single samples in cells with mixed labels
+    float gr[M][32];   // each lane's material weights gr_m
+    float ray[9][32];  // each lane's unit ray in IJK (0-2), source in IJK (3-5), unit ray in world (6-8)
+    float A[9];        // the view's IJK_from_world rotation
+};
+
+__device__ __forceinline__ void red_add_pair(float *a, float x, float y) {
+    if ((reinterpret_cast<uintptr_t>(a) & 7u) == 0) {
+        asm volatile("red.global.add.v2.f32 [%0], {%1, %2};" ::"l"(a), "f"(x), "f"(y) : "memory");
+    } else {
+        if (x != 0.0f) atomicAdd(a, x);
+        if (y != 0.0f) atomicAdd(a + 1, y);
+    }
+}
+
+// Adds v[c] to texel c = dx | dy << 1 | dz << 2 of the filter cell with lower corner (i0, j0, k0):
+// texel (min(i0 + dx, n0 - 1), ...) of the [n2][n1][n0] gradient volume, as the texture's clamp
+// addressing reads it. The two texels of a row are adjacent and go out as one vector reduction.
+__device__ __forceinline__ void scatter_cell(float *grad, int i0, int j0, int k0, int n0, int n1, int n2,
+                                             const float v[8]) {
+    const int j1 = min(j0 + 1, n1 - 1), k1 = min(k0 + 1, n2 - 1);
+#pragma unroll
+    for (int row = 0; row < 4; row++) {
+        const int j = row & 1 ? j1 : j0, k = row & 2 ? k1 : k0;
+        const float x = v[2 * row], y = v[2 * row + 1];
+        float *a = grad + ((size_t)k * n1 + j) * n0 + i0;
+        if (i0 + 1 >= n0) {  // clamped edge: both corners are the same texel
+            if (x + y != 0.0f) atomicAdd(a, x + y);
+        } else if (x != 0.0f || y != 0.0f) {
+            red_add_pair(a, x, y);
+        }
+    }
+}
+
+// Density and pose gradients of one view per blockIdx.z, one ray per thread (16 x 8 pixel tiles,
+// each warp 8 x 4 pixels). A run is a stretch of a ray's samples with one label cell, one
+// texture-filter cell and one trapezoid weight; see the file comment. 5 blocks per SM (96
+// registers) balances occupancy against the registers the drain needs.
+template <int M>
+__global__ void __launch_bounds__(kBlockThreads, 5) adjoint_kernel(const __grid_constant__ AdjointParams P) {
+    __shared__ AdjointWarpSmem<M> smem[kBlockThreads / 32];
     const SceneParams<1> &p = P.s;
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
+    AdjointWarpSmem<M> &sh = smem[warp];
     const int u = blockIdx.x * kTileW + ((warp & 1) << 3) + (lane & 7);
     const int v = blockIdx.y * kTileH + ((warp >> 1) << 2) + (lane >> 3);
-    const int zv = blockIdx.z;
-    if (u >= p.width || v >= p.height || zv >= P.n_views) return;
-    AdjointRay<M> R;
-    if (!adjoint_setup<M>(P, P.views[zv], u, v, zv, R)) return;
+    const int zv = blockIdx.z;  // the grid has one z per view
+    const AdjointView &av = P.views[zv];
     const VolConst &V = p.vol[0];
+    const bool do_dens = P.grad_density != nullptr;
+    const bool do_pose = P.grad_pose != nullptr;
+    const unsigned kAll = 0xffffffffu;
+
+    AdjointRay<M> R{};
+    bool live = u < p.width && v < p.height && adjoint_setup<M>(P, av, u, v, zv, R);
+#pragma unroll
+    for (int m = 0; m < M; m++) sh.gr[m][lane] = live ? R.gr[m] : 0.0f;
+    sh.ray[0][lane] = R.rxi;
+    sh.ray[1][lane] = R.ryi;
+    sh.ray[2][lane] = R.rzi;
+    sh.ray[3][lane] = R.sx;
+    sh.ray[4][lane] = R.sy;
+    sh.ray[5][lane] = R.sz;
+    sh.ray[6][lane] = R.rx;
+    sh.ray[7][lane] = R.ry;
+    sh.ray[8][lane] = R.rz;
+    if (lane < 9) sh.A[lane] = av.v.vol[0].a[lane];
+    __syncwarp();
+
     const int n0 = V.n[0], n1 = V.n[1], n2 = V.n[2];
     const float step = p.step;
     float *const grad = P.grad_density;
-    float alpha = R.alpha;
-    // label words are loaded one step ahead (as in the forward) so no lane branches to fetch them;
-    // the material weight of a uniform cell is cached while the label stays the same
-    int cur_label = -1;
-    float cur_g = 0.0f;
-    // hardware-filter cell and its sums
-    int ci = -1, cj = 0, ck = 0, ci1 = 0, cj1 = 0, ck1 = 0;
-    float acc[8];
-    int iw[8];
-#pragma unroll
-    for (int c = 0; c < 8; c++) acc[c] = 0.0f, iw[c] = 0;
-    float run = 0.0f;  // w_t q_t / 256 of the integer sums in iw
-    auto fold = [&]() {
-#pragma unroll
-        for (int c = 0; c < 8; c++) {
-            acc[c] = __fmaf_rn(run, (float)iw[c], acc[c]);
-            iw[c] = 0;
-        }
-    };
-    auto flush = [&]() {
-        fold();
-        const int is[2] = {ci, ci1}, js[2] = {cj, cj1}, ks[2] = {ck, ck1};
-#pragma unroll
-        for (int c = 0; c < 8; c++) {
-            if (acc[c] != 0.0f) atomicAdd(grad + ((size_t)ks[c >> 2] * n1 + js[(c >> 1) & 1]) * n0 + is[c & 1], acc[c]);
-            acc[c] = 0.0f;
-        }
-    };
-    float cx = __fsub_rn(__fmaf_rn(alpha, R.rxi, R.sx), 1.0f);
-    float cy = __fsub_rn(__fmaf_rn(alpha, R.ryi, R.sy), 1.0f);
-    float cz = __fsub_rn(__fmaf_rn(alpha, R.rzi, R.sz), 1.0f);
-    float cbx = floorf(cx), cby = floorf(cy), cbz = floorf(cz);
-    uint32_t w_cur = fetch_label_word(V, cbx, cby, cbz);
-    for (int t = R.t; t < R.t_end; ++t) {
-        const float wt = (0 == t || R.num_steps - 1 == t) ? 0.5f : 1.0f;
-        const float an = __fadd_rn(alpha, step);
-        const float nx = __fsub_rn(__fmaf_rn(an, R.rxi, R.sx), 1.0f);
-        const float ny = __fsub_rn(__fmaf_rn(an, R.ryi, R.sy), 1.0f);
-        const float nz = __fsub_rn(__fmaf_rn(an, R.rzi, R.sz), 1.0f);
-        const float nbx = floorf(nx), nby = floorf(ny), nbz = floorf(nz);
-        const uint32_t w_next = fetch_label_word(V, nbx, nby, nbz);
-        const float px = cx, py = cy, pz = cz;
-        const uint32_t word = w_cur;
-        float q;
-        if (uniform_word(word)) {
-            const int L = (int)(word & 15u);
-            if (L != cur_label) {
-                cur_label = L;
-                cur_g = gr_of<M>(R.gr, L);
-            }
-            q = cur_g;
-        } else {
-            const CornerWeights cw = corner_weights(__fsub_rn(px, cbx), __fsub_rn(py, cby), __fsub_rn(pz, cbz));
-            const uint32_t A = word & 15u;
-            const uint32_t xa = word ^ (A * 0x11111111u);
-            const uint32_t B = (word >> ((__ffs(xa) - 1) & ~3)) & 15u;
-            const uint32_t xb = word ^ (B * 0x11111111u);
-            const uint32_t za = ~(((xa & 0x77777777u) + 0x77777777u) | xa) & 0x88888888u;
-            const uint32_t zb = ~(((xb & 0x77777777u) + 0x77777777u) | xb) & 0x88888888u;
-            if ((za | zb) == 0x88888888u) {
-                float sA = 0.0f, sB = 0.0f;
-#pragma unroll
-                for (int c = 0; c < 8; c++) {
-                    const float w = __fmul_rn(cw.xy[c & 3], cw.z[c >> 2]);
-                    if ((za >> (4 * c + 3)) & 1u)
-                        sA += w;
-                    else
-                        sB += w;
-                }
-                q = __fmaf_rn(sA, gr_of<M>(R.gr, (int)A), sB * gr_of<M>(R.gr, (int)B));
-            } else {
-                q = 0.0f;
-#pragma unroll
-                for (int c = 0; c < 8; c++)
-                    q = __fmaf_rn(__fmul_rn(cw.xy[c & 3], cw.z[c >> 2]), gr_of<M>(R.gr, (int)((word >> (4 * c)) & 15u)),
-                                  q);
-            }
-        }
-        int i0, i1, ax_, j0, j1, ay_, k0, k1, az_;
-        hw_axis(__fadd_rn(px, 0.5f), n0, i0, i1, ax_);
-        hw_axis(__fadd_rn(py, 0.5f), n1, j0, j1, ay_);
-        hw_axis(__fadd_rn(pz, 0.5f), n2, k0, k1, az_);
-        if (i0 != ci || j0 != cj || k0 != ck) {
-            if (ci >= 0) flush();
-            ci = i0, cj = j0, ck = k0, ci1 = i1, cj1 = j1, ck1 = k1;
-        }
-        const float r = wt * q * (1.0f / 256.0f);
-        if (r != run) {
-            fold();
-            run = r;
-        }
-        int W[8];
-        hw_weights(ax_, ay_, az_, W);
-#pragma unroll
-        for (int c = 0; c < 8; c++) iw[c] += W[c];
-        alpha = an;
-        cx = nx, cy = ny, cz = nz, cbx = nbx, cby = nby, cbz = nbz;
-        w_cur = w_next;
-    }
-    if (ci >= 0) flush();
-}
+    float Hs0 = 0.0f, Hs1 = 0.0f, Hs2 = 0.0f, Cs0 = 0.0f, Cs1 = 0.0f, Cs2 = 0.0f;
 
-// Pose gradient: d/dp of w_t rho(p) Q(p) with rho and Q the continuous trilinear interpolants of the
-// label cell's texels and per-corner material weights, summed as q_w = A^T h (Hw) and alpha q_w (K).
-// In a cell whose eight labels agree Q is constant and grad rho is bilinear in the fractions, so the
-// cell's samples are summed as weighted moments of the fractions and turned into h when the ray
-// leaves the cell; mixed cells are evaluated per sample.
-template <int M>
-__global__ void __launch_bounds__(kBlockThreads) adjoint_pose_kernel(const __grid_constant__ AdjointParams P) {
-    const SceneParams<1> &p = P.s;
-    const int lane = threadIdx.x & 31;
-    const int warp = threadIdx.x >> 5;
-    const int u = blockIdx.x * kTileW + ((warp & 1) << 3) + (lane & 7);
-    const int v = blockIdx.y * kTileH + ((warp >> 1) << 2) + (lane >> 3);
-    const int zv = blockIdx.z;
-    const bool active = u < p.width && v < p.height && zv < P.n_views;
-    float pose[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    AdjointRay<M> R;
-    if (active && adjoint_setup<M>(P, P.views[zv], u, v, zv, R)) {
-        const VolConst &V = p.vol[0];
-        const float step = p.step;
-        float alpha = R.alpha;
-        float pb0 = __int_as_float(0x7fc00000), pb1 = pb0, pb2 = pb0;
-        bool uni = false;
-        float gu = 0.0f, g8[8], rho8[8];
+    // r_owner x (A^T hk) in world coordinates, and the IJK sum h, into this lane's pose sums
+    auto add_pose = [&](const float h[3], const float hk[3], int owner) {
+        Hs0 += h[0], Hs1 += h[1], Hs2 += h[2];
+        const float kx = sh.A[0] * hk[0] + sh.A[3] * hk[1] + sh.A[6] * hk[2];
+        const float ky = sh.A[1] * hk[0] + sh.A[4] * hk[1] + sh.A[7] * hk[2];
+        const float kz = sh.A[2] * hk[0] + sh.A[5] * hk[1] + sh.A[8] * hk[2];
+        const float ox = sh.ray[6][owner], oy = sh.ray[7][owner], oz = sh.ray[8][owner];
+        Cs0 += oy * kz - oz * ky;
+        Cs1 += oz * kx - ox * kz;
+        Cs2 += ox * ky - oy * kx;
+    };
+
+    // Drains `count` (<= 32) queued uniform-label runs starting at ring slot `first`, one run per
+    // lane. Each run is re-derived from its first alpha with the march's own float32 operations, so
+    // its positions, label cell and filter cell are the march's.
+    auto drain_runs = [&](int first, int count) {
+        if (lane >= count) return;
+        const int e = (first + lane) & (kAdjQueue - 1);
+        const float al = __uint_as_float(sh.run[0][e]);
+        const uint32_t w1 = sh.run[1][e];
+        const int kn = (int)(w1 & 255u), owner = (int)((w1 >> 8) & 31u);
+        const float wrun = (w1 >> 13) & 1u ? 0.5f : 1.0f;
+        const uint32_t word = sh.run[2][e];
+        const float rxi = sh.ray[0][owner], ryi = sh.ray[1][owner], rzi = sh.ray[2][owner];
+        const float sx = sh.ray[3][owner], sy = sh.ray[4][owner], sz = sh.ray[5][owner];
+        const float px = __fsub_rn(__fmaf_rn(al, rxi, sx), 1.0f);
+        const float py = __fsub_rn(__fmaf_rn(al, ryi, sy), 1.0f);
+        const float pz = __fsub_rn(__fmaf_rn(al, rzi, sz), 1.0f);
+        const float bx = floorf(px), by = floorf(py), bz = floorf(pz);
+        const int fxi = hw_fix_from_floor(__float2int_rd(__fmaf_rn(__fadd_rn(px, 0.5f), 256.0f, -127.5f)), n0);
+        const int fyi = hw_fix_from_floor(__float2int_rd(__fmaf_rn(__fadd_rn(py, 0.5f), 256.0f, -127.5f)), n1);
+        const int fzi = hw_fix_from_floor(__float2int_rd(__fmaf_rn(__fadd_rn(pz, 0.5f), 256.0f, -127.5f)), n2);
+        float h[3], hk[3];
+        float r8[8];
+        if (do_pose) {
 #pragma unroll
-        for (int c = 0; c < 8; c++) g8[c] = rho8[c] = 0.0f;
-        // moments of the current uniform cell: sum w, w f_x, w f_y, w f_z, w f_x f_y, w f_x f_z,
-        // w f_y f_z, and the same weighted by alpha
-        float m[7], n[7];
-#pragma unroll
-        for (int k = 0; k < 7; k++) m[k] = n[k] = 0.0f;
-        // sums of h and alpha h in IJK space; the world-space q = A^T h is applied once per ray
-        float Hi[3] = {0.f, 0.f, 0.f}, Ki[3] = {0.f, 0.f, 0.f};
-        auto add_world = [&](float hx, float hy, float hz, float kx, float ky, float kz) {
-            Hi[0] += hx, Hi[1] += hy, Hi[2] += hz;
-            Ki[0] += kx, Ki[1] += ky, Ki[2] += kz;
-        };
-        auto flush_moments = [&]() {
-            if (m[0] == 0.0f) return;
-            const float *r = rho8;
-            const float dx0 = r[1] - r[0], dx1 = r[3] - r[2], dx2 = r[5] - r[4], dx3 = r[7] - r[6];
-            const float dy0 = r[2] - r[0], dy1 = r[3] - r[1], dy2 = r[6] - r[4], dy3 = r[7] - r[5];
-            const float dz0 = r[4] - r[0], dz1 = r[5] - r[1], dz2 = r[6] - r[2], dz3 = r[7] - r[3];
-            // d rho / d f_x = dx0 + (dx1 - dx0) f_y + (dx2 - dx0) f_z + (dx0 - dx1 - dx2 + dx3) f_y f_z, etc.
-            auto gsum = [&](const float *s) {
-                float g[3];
-                g[0] = dx0 * s[0] + (dx1 - dx0) * s[2] + (dx2 - dx0) * s[3] + (dx0 - dx1 - dx2 + dx3) * s[6];
-                g[1] = dy0 * s[0] + (dy1 - dy0) * s[1] + (dy2 - dy0) * s[3] + (dy0 - dy1 - dy2 + dy3) * s[5];
-                g[2] = dz0 * s[0] + (dz1 - dz0) * s[1] + (dz2 - dz0) * s[2] + (dz0 - dz1 - dz2 + dz3) * s[4];
-                return make_float3(g[0] * gu, g[1] * gu, g[2] * gu);
-            };
-            const float3 h = gsum(m), hk = gsum(n);
-            add_world(h.x, h.y, h.z, hk.x, hk.y, hk.z);
-#pragma unroll
-            for (int k = 0; k < 7; k++) m[k] = n[k] = 0.0f;
-        };
-        for (int t = R.t; t < R.t_end; ++t) {
-            const float wt = (0 == t || R.num_steps - 1 == t) ? 0.5f : 1.0f;
-            const float px = __fsub_rn(__fmaf_rn(alpha, R.rxi, R.sx), 1.0f);
-            const float py = __fsub_rn(__fmaf_rn(alpha, R.ryi, R.sy), 1.0f);
-            const float pz = __fsub_rn(__fmaf_rn(alpha, R.rzi, R.sz), 1.0f);
-            const float bx = floorf(px), by = floorf(py), bz = floorf(pz);
-            const float fx = __fsub_rn(px, bx), fy = __fsub_rn(py, by), fz = __fsub_rn(pz, bz);
-            if (bx != pb0 || by != pb1 || bz != pb2) {
-                if (uni) flush_moments();
-                const uint32_t word = fetch_label_word(V, bx, by, bz);
-                uni = uniform_word(word);
-                gu = gr_of<M>(R.gr, (int)(word & 15u));
-                if (!uni) {
-#pragma unroll
-                    for (int c = 0; c < 8; c++) g8[c] = gr_of<M>(R.gr, (int)((word >> (4 * c)) & 15u));
-                }
-#pragma unroll
-                for (int c = 0; c < 8; c++)
-                    rho8[c] = tex3D<float>(P.density_point, bx + (float)(c & 1) + 0.5f,
-                                           by + (float)((c >> 1) & 1) + 0.5f, bz + (float)(c >> 2) + 0.5f);
-                pb0 = bx, pb1 = by, pb2 = bz;
-            }
-            if (uni) {
-                if (gu != 0.0f) {
-                    const float wa = wt * alpha;
-                    const float fxy = fx * fy, fxz = fx * fz, fyz = fy * fz;
-                    m[0] += wt, m[1] += wt * fx, m[2] += wt * fy, m[3] += wt * fz;
-                    m[4] += wt * fxy, m[5] += wt * fxz, m[6] += wt * fyz;
-                    n[0] += wa, n[1] += wa * fx, n[2] += wa * fy, n[3] += wa * fz;
-                    n[4] += wa * fxy, n[5] += wa * fxz, n[6] += wa * fyz;
-                }
-            } else {
-                const float gx = 1.0f - fx, gy = 1.0f - fy, gz = 1.0f - fz;
-                float dr[3], dQ[3];
-                trilinear_grad(rho8, fx, fy, fz, gx, gy, gz, dr);
-                trilinear_grad(g8, fx, fy, fz, gx, gy, gz, dQ);
-                const float rho = trilinear(rho8, fx, fy, fz, gx, gy, gz);
-                const float Q = trilinear(g8, fx, fy, fz, gx, gy, gz);
-                const float hx = wt * (dr[0] * Q + rho * dQ[0]);
-                const float hy = wt * (dr[1] * Q + rho * dQ[1]);
-                const float hz = wt * (dr[2] * Q + rho * dQ[2]);
-                add_world(hx, hy, hz, alpha * hx, alpha * hy, alpha * hz);
-            }
-            alpha = __fadd_rn(alpha, step);
+            for (int c = 0; c < 8; c++)
+                r8[c] = tex3D<float>(P.density_point, bx + (float)(c & 1) + 0.5f, by + (float)((c >> 1) & 1) + 0.5f,
+                                     bz + (float)(c >> 2) + 0.5f);
         }
-        if (uni) flush_moments();
-        float Hw[3], K[3];
+        const float gu = sh.gr[word & 15u][owner];
+        if (do_dens) {
+            // every sample of the run adds w_t gu W_c / 256 to texel c: the packed sums hold sum W_c
+            const float rv = __fmul_rn(__fmul_rn(wrun, gu), 1.0f / 256.0f);
+            float vals[8];
 #pragma unroll
-        for (int k = 0; k < 3; k++) {
-            Hw[k] = R.A[k] * Hi[0] + R.A[3 + k] * Hi[1] + R.A[6 + k] * Hi[2];
-            K[k] = R.A[k] * Ki[0] + R.A[3 + k] * Ki[1] + R.A[6 + k] * Ki[2];
+            for (int row = 0; row < 4; row++) {
+                // packed word of (dx, dy) holds dz = 0 | dz = 1 << 16
+                const int dy = row & 1, dz = row >> 1;
+                const uint32_t s0 = sh.run[3 + dy][e], s1 = sh.run[5 + dy][e];
+                vals[2 * row] = rv * (float)((s0 >> (16 * dz)) & 0xFFFFu);
+                vals[2 * row + 1] = rv * (float)((s1 >> (16 * dz)) & 0xFFFFu);
+            }
+            scatter_cell(grad, fxi >> 8, fyi >> 8, fzi >> 8, n0, n1, n2, vals);
         }
-        const float d[3] = {P.views[zv].source_world[0] - P.center[0], P.views[zv].source_world[1] - P.center[1],
-                            P.views[zv].source_world[2] - P.center[2]};
-        const float rr[3] = {R.rx, R.ry, R.rz};
-        pose[0] = -Hw[0];
-        pose[1] = -Hw[1];
-        pose[2] = -Hw[2];
-        pose[3] = -((d[1] * Hw[2] - d[2] * Hw[1]) + (rr[1] * K[2] - rr[2] * K[1]));
-        pose[4] = -((d[2] * Hw[0] - d[0] * Hw[2]) + (rr[2] * K[0] - rr[0] * K[2]));
-        pose[5] = -((d[0] * Hw[1] - d[1] * Hw[0]) + (rr[0] * K[1] - rr[1] * K[0]));
+        if (do_pose) {
+            // grad rho = c0 + c1 f_a + c2 f_b + c3 f_a f_b per axis (f_a, f_b the other two
+            // fractions), summed over the run's samples f0 + k d, alpha0 + k delta in closed form
+            const float ax = __fsub_rn(px, bx), ay = __fsub_rn(py, by), az = __fsub_rn(pz, bz);
+            const float delta = __fsub_rn(__fadd_rn(al, step), al);  // the float32 step at alpha0
+            const float bxs = delta * rxi, bys = delta * ryi, bzs = delta * rzi;
+            const float ex = r8[1] - r8[0], ey = r8[2] - r8[0], ez = r8[4] - r8[0];
+            const float x1 = (r8[3] - r8[2]) - ex, x2 = (r8[5] - r8[4]) - ex;
+            const float x3 = (r8[7] - r8[6]) - (r8[5] - r8[4]) - (r8[3] - r8[2]) + ex;
+            const float y1 = (r8[3] - r8[1]) - ey, y2 = (r8[6] - r8[4]) - ey;
+            const float y3 = (r8[7] - r8[5]) - (r8[6] - r8[4]) - (r8[3] - r8[1]) + ey;
+            const float z1 = (r8[5] - r8[1]) - ez, z2 = (r8[6] - r8[2]) - ez;
+            const float z3 = (r8[7] - r8[3]) - (r8[6] - r8[2]) - (r8[5] - r8[1]) + ez;
+            const float kf = (float)kn;
+            const float T1 = 0.5f * kf * (kf - 1.0f);                   // sum k
+            const float T2 = T1 * (2.0f * kf - 1.0f) * (1.0f / 3.0f);  // sum k^2
+            const float T3 = T1 * T1;                                   // sum k^3
+            // moment of g: m = sum g(f_k), n = sum alpha_k g(f_k) = alpha0 m + delta sum k g(f_k)
+            float m = kf, n = al * kf + delta * T1;  // g = 1
+            h[0] = ex * m, h[1] = ey * m, h[2] = ez * m;
+            hk[0] = ex * n, hk[1] = ey * n, hk[2] = ez * n;
+            m = kf * ax + bxs * T1, n = al * m + delta * (ax * T1 + bxs * T2);  // g = f_x
+            h[1] += y1 * m, h[2] += z1 * m, hk[1] += y1 * n, hk[2] += z1 * n;
+            m = kf * ay + bys * T1, n = al * m + delta * (ay * T1 + bys * T2);  // g = f_y
+            h[0] += x1 * m, h[2] += z2 * m, hk[0] += x1 * n, hk[2] += z2 * n;
+            m = kf * az + bzs * T1, n = al * m + delta * (az * T1 + bzs * T2);  // g = f_z
+            h[0] += x2 * m, h[1] += y2 * m, hk[0] += x2 * n, hk[1] += y2 * n;
+            float c0 = ax * ay, c1 = ax * bys + ay * bxs, c2 = bxs * bys;  // g = f_x f_y
+            m = kf * c0 + c1 * T1 + c2 * T2, n = al * m + delta * (c0 * T1 + c1 * T2 + c2 * T3);
+            h[2] += z3 * m, hk[2] += z3 * n;
+            c0 = ax * az, c1 = ax * bzs + az * bxs, c2 = bxs * bzs;  // g = f_x f_z
+            m = kf * c0 + c1 * T1 + c2 * T2, n = al * m + delta * (c0 * T1 + c1 * T2 + c2 * T3);
+            h[1] += y3 * m, hk[1] += y3 * n;
+            c0 = ay * az, c1 = ay * bzs + az * bys, c2 = bys * bzs;  // g = f_y f_z
+            m = kf * c0 + c1 * T1 + c2 * T2, n = al * m + delta * (c0 * T1 + c1 * T2 + c2 * T3);
+            h[0] += x3 * m, hk[0] += x3 * n;
+            const float gw = gu * wrun;
+#pragma unroll
+            for (int c = 0; c < 3; c++) h[c] *= gw, hk[c] *= gw;
+        }
+        if (do_pose) add_pose(h, hk, owner);
+    };
+
+    // Drains `count` (<= 32) queued mixed-label samples starting at ring slot `first`, one per lane:
+    // the forward's label weights q_t, the texture unit's corner weights for the density, and the
+    // trilinear gradient of rho Q for the pose.
+    auto drain_mixed = [&](int first, int count) {
+        if (lane >= count) return;
+        const int e = (first + lane) & (kAdjQueue - 1);
+        const float al = __uint_as_float(sh.mix[0][e]);
+        const uint32_t w1 = sh.mix[1][e];
+        const int owner = (int)((w1 >> 8) & 31u);
+        const float wrun = (w1 >> 13) & 1u ? 0.5f : 1.0f;
+        const uint32_t word = sh.mix[2][e];
+        const float px = __fsub_rn(__fmaf_rn(al, sh.ray[0][owner], sh.ray[3][owner]), 1.0f);
+        const float py = __fsub_rn(__fmaf_rn(al, sh.ray[1][owner], sh.ray[4][owner]), 1.0f);
+        const float pz = __fsub_rn(__fmaf_rn(al, sh.ray[2][owner], sh.ray[5][owner]), 1.0f);
+        const float bx = floorf(px), by = floorf(py), bz = floorf(pz);
+        const float fx = __fsub_rn(px, bx), fy = __fsub_rn(py, by), fz = __fsub_rn(pz, bz);
+        float g8[8];
+#pragma unroll
+        for (int c = 0; c < 8; c++) g8[c] = sh.gr[(word >> (4 * c)) & 15u][owner];
+        if (do_dens) {
+            const CornerWeights cw = corner_weights(fx, fy, fz);
+            float q = 0.0f;
+#pragma unroll
+            for (int c = 0; c < 8; c++) q = __fmaf_rn(__fmul_rn(cw.xy[c & 3], cw.z[c >> 2]), g8[c], q);
+            const float rv = __fmul_rn(__fmul_rn(wrun, q), 1.0f / 256.0f);
+            const int fxi = hw_fix_from_floor(__float2int_rd(__fmaf_rn(__fadd_rn(px, 0.5f), 256.0f, -127.5f)), n0);
+            const int fyi = hw_fix_from_floor(__float2int_rd(__fmaf_rn(__fadd_rn(py, 0.5f), 256.0f, -127.5f)), n1);
+            const int fzi = hw_fix_from_floor(__float2int_rd(__fmaf_rn(__fadd_rn(pz, 0.5f), 256.0f, -127.5f)), n2);
+            int W[8];
+            hw_corner_weights(fxi & 255, fyi & 255, fzi & 255, W);
+            float vals[8];
+#pragma unroll
+            for (int c = 0; c < 8; c++) vals[c] = rv * (float)W[c];
+            scatter_cell(grad, fxi >> 8, fyi >> 8, fzi >> 8, n0, n1, n2, vals);
+        }
+        if (do_pose) {
+            float r8[8];
+#pragma unroll
+            for (int c = 0; c < 8; c++)
+                r8[c] = tex3D<float>(P.density_point, bx + (float)(c & 1) + 0.5f, by + (float)((c >> 1) & 1) + 0.5f,
+                                     bz + (float)(c >> 2) + 0.5f);
+            const float gx = 1.0f - fx, gy = 1.0f - fy, gz = 1.0f - fz;
+            float dr[3], dQ[3];
+            trilinear_grad(r8, fx, fy, fz, gx, gy, gz, dr);
+            trilinear_grad(g8, fx, fy, fz, gx, gy, gz, dQ);
+            const float rho = trilinear(r8, fx, fy, fz, gx, gy, gz);
+            const float Q = trilinear(g8, fx, fy, fz, gx, gy, gz);
+            float h[3], hk[3];
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                h[c] = wrun * (dr[c] * Q + rho * dQ[c]);
+                hk[c] = al * h[c];
+            }
+            add_pose(h, hk, owner);
+        }
+    };
+
+    float alpha = R.alpha;
+    int t = R.t;
+    const int t_end = R.t_end, t_last = R.num_steps - 1;
+    // the current sample: position, label cell and label word (the next word is loaded a step ahead)
+    float cx = 0.0f, cy = 0.0f, cz = 0.0f, cbx = 0.0f, cby = 0.0f, cbz = 0.0f;
+    uint32_t w_cur = 0;
+    if (live) {
+        cx = __fsub_rn(__fmaf_rn(alpha, R.rxi, R.sx), 1.0f);
+        cy = __fsub_rn(__fmaf_rn(alpha, R.ryi, R.sy), 1.0f);
+        cz = __fsub_rn(__fmaf_rn(alpha, R.rzi, R.sz), 1.0f);
+        cbx = floorf(cx), cby = floorf(cy), cbz = floorf(cz);
+        w_cur = fetch_label_word(V, cbx, cby, cbz);
     }
-    if (zv < P.n_views) {
-        // one view per block: reduce over the warp, then one atomic per warp and component
+    // the open run: sample count, first alpha, label cell, filter fixed point, weight, packed sums
+    int K = 0;
+    float a0 = 0.0f, rbx = 0.0f, rby = 0.0f, rbz = 0.0f, rw = 0.0f;
+    int rfx = 0, rfy = 0, rfz = 0;
+    uint32_t rword = 0, S0 = 0, S1 = 0, S2 = 0, S3 = 0;
+    bool rmixed = false;       // the open run is one sample of a mixed-label cell
+    int head = 0, queued = 0;  // warp-uniform ring state of the uniform-label runs
+    int mhead = 0, mqueued = 0;  // and of the mixed-label samples
+    const unsigned lt = (1u << lane) - 1u;
+
+    for (;;) {
+        const bool have = live;
+        bool fresh = false;
+        int fxi = 0, fyi = 0, fzi = 0;
+        float wt = 1.0f, an = 0.0f, nx = 0.0f, ny = 0.0f, nz = 0.0f, nbx = 0.0f, nby = 0.0f, nbz = 0.0f;
+        uint32_t w_next = 0;
+        if (have) {
+            an = __fadd_rn(alpha, step);
+            nx = __fsub_rn(__fmaf_rn(an, R.rxi, R.sx), 1.0f);
+            ny = __fsub_rn(__fmaf_rn(an, R.ryi, R.sy), 1.0f);
+            nz = __fsub_rn(__fmaf_rn(an, R.rzi, R.sz), 1.0f);
+            nbx = floorf(nx), nby = floorf(ny), nbz = floorf(nz);
+            w_next = fetch_label_word(V, nbx, nby, nbz);
+            wt = (0 == t || t_last == t) ? 0.5f : 1.0f;
+            fresh = K == 0 || K == 255 || rmixed || cbx != rbx || cby != rby || cbz != rbz || wt != rw;
+            if (do_dens) {
+                // texture-unit fixed point of the density coordinate p + 0.5 (drr_texweights.h)
+                fxi = hw_fix_from_floor(__float2int_rd(__fmaf_rn(__fadd_rn(cx, 0.5f), 256.0f, -127.5f)), n0);
+                fyi = hw_fix_from_floor(__float2int_rd(__fmaf_rn(__fadd_rn(cy, 0.5f), 256.0f, -127.5f)), n1);
+                fzi = hw_fix_from_floor(__float2int_rd(__fmaf_rn(__fadd_rn(cz, 0.5f), 256.0f, -127.5f)), n2);
+                fresh = fresh || ((fxi ^ rfx) | (fyi ^ rfy) | (fzi ^ rfz)) >= 256;
+            }
+        }
+        // a run ends when the next sample starts a new one or the ray has no samples left
+        const bool push = K > 0 && (!have || fresh);
+        const unsigned pm = __ballot_sync(kAll, push && !rmixed);
+        const unsigned mm = __ballot_sync(kAll, push && rmixed);
+        if (push) {
+            const uint32_t tag = ((uint32_t)lane << 8) | (rw != 1.0f ? 1u << 13 : 0u);
+            if (!rmixed) {
+                const int s = (head + queued + __popc(pm & lt)) & (kAdjQueue - 1);
+                sh.run[0][s] = __float_as_uint(a0);
+                sh.run[1][s] = (uint32_t)K | tag;
+                sh.run[2][s] = rword;
+                sh.run[3][s] = S0;
+                sh.run[4][s] = S1;
+                sh.run[5][s] = S2;
+                sh.run[6][s] = S3;
+            } else {
+                const int s = (mhead + mqueued + __popc(mm & lt)) & (kAdjQueue - 1);
+                sh.mix[0][s] = __float_as_uint(a0);
+                sh.mix[1][s] = tag;
+                sh.mix[2][s] = rword;
+            }
+            K = 0;
+        }
+        queued += __popc(pm);
+        mqueued += __popc(mm);
+        if (have) {
+            if (K == 0) {
+                a0 = alpha;
+                rbx = cbx, rby = cby, rbz = cbz;
+                rfx = fxi, rfy = fyi, rfz = fzi;
+                rw = wt;
+                rword = w_cur;
+                rmixed = !uniform_word(w_cur);
+                S0 = S1 = S2 = S3 = 0u;
+            }
+            if (do_dens) {
+                uint32_t Wp[4];
+                packed_corner_weights((uint32_t)fxi & 255u, (uint32_t)fyi & 255u, (uint32_t)fzi & 255u, Wp);
+                S0 += Wp[0], S1 += Wp[1], S2 += Wp[2], S3 += Wp[3];
+            }
+            ++K;
+            ++t;
+            alpha = an;
+            cx = nx, cy = ny, cz = nz, cbx = nbx, cby = nby, cbz = nbz;
+            w_cur = w_next;
+            live = t < t_end;
+        }
+        if (queued >= 32) {
+            __syncwarp();
+            drain_runs(head, 32);
+            __syncwarp();
+            head = (head + 32) & (kAdjQueue - 1);
+            queued -= 32;
+        }
+        if (mqueued >= 32) {
+            __syncwarp();
+            drain_mixed(mhead, 32);
+            __syncwarp();
+            mhead = (mhead + 32) & (kAdjQueue - 1);
+            mqueued -= 32;
+        }
+        if (!__any_sync(kAll, live || K > 0)) break;
+    }
+    __syncwarp();
+    drain_runs(head, queued);
+    drain_mixed(mhead, mqueued);
+
+    if (do_pose) {
+        // the warp's pose sums: one atomic per component
 #pragma unroll
-        for (int k = 0; k < 6; k++) {
-            float x = pose[k];
-            for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-            if (lane == 0 && x != 0.0f) atomicAdd(P.grad_pose + (size_t)zv * 6 + k, x);
+        for (int o = 16; o > 0; o >>= 1) {
+            Hs0 += __shfl_xor_sync(kAll, Hs0, o);
+            Hs1 += __shfl_xor_sync(kAll, Hs1, o);
+            Hs2 += __shfl_xor_sync(kAll, Hs2, o);
+            Cs0 += __shfl_xor_sync(kAll, Cs0, o);
+            Cs1 += __shfl_xor_sync(kAll, Cs1, o);
+            Cs2 += __shfl_xor_sync(kAll, Cs2, o);
+        }
+        if (lane == 0) {
+            const float *A = sh.A;
+            const float Hw[3] = {A[0] * Hs0 + A[3] * Hs1 + A[6] * Hs2, A[1] * Hs0 + A[4] * Hs1 + A[7] * Hs2,
+                                 A[2] * Hs0 + A[5] * Hs1 + A[8] * Hs2};
+            const float d[3] = {av.source_world[0] - P.center[0], av.source_world[1] - P.center[1],
+                                av.source_world[2] - P.center[2]};
+            const float pose[6] = {-Hw[0], -Hw[1], -Hw[2], -((d[1] * Hw[2] - d[2] * Hw[1]) + Cs0),
+                                   -((d[2] * Hw[0] - d[0] * Hw[2]) + Cs1), -((d[0] * Hw[1] - d[1] * Hw[0]) + Cs2)};
+#pragma unroll
+            for (int k = 0; k < 6; k++)
+                if (pose[k] != 0.0f) atomicAdd(P.grad_pose + (size_t)zv * 6 + k, pose[k]);
         }
     }
 }

@@ -554,6 +554,11 @@ extern "C" drr_status drr_project_adjoint(drr_volset *set, const drr_tables *tab
     drr_status st = validate(set, tables, &a);
     if (st != DRR_OK) return st;
     if (!args->enabled[0]) return fail(DRR_ERR_INVALID_ARGUMENT, "drr_project_adjoint: the volume is disabled");
+    {
+        const drr::Volume &v = set->vol[0];
+        if (v.ni > 32767 || v.nj > 32767 || v.nk > 32767)
+            return fail(DRR_ERR_UNSUPPORTED, "drr_project_adjoint: volumes above 32767 voxels per axis");
+    }
     if (args->n_views == 0 || (!adj->grad_density && !adj->grad_pose)) return DRR_OK;
     cudaStream_t s = (cudaStream_t)stream;
     st = ensure_point_texture(set->vol[0]);
