@@ -170,13 +170,11 @@ __device__ __forceinline__ bool adjoint_setup(const AdjointParams &P, const Adjo
 // Per-warp run queue of adjoint_kernel: a ring of kAdjQueue entries (structure of arrays, word k
 // of entry e at [k][e]); the warp drains 32 runs at a time.
 constexpr int kAdjQueue = 64;
-constexpr int kRunWords = 7;  // alpha0, count | lane << 8 | half << 13, label word, four packed corner sums
-constexpr int kMixWords = 3;  // alpha, lane << 8 | half << 13, label word
+constexpr int kRunWords = 6;  // alpha0, count | lane << 8 | half << 13, four packed corner sums
 
 template <int M>
 struct AdjointWarpSmem {
-    uint32_t run[kRunWords][kAdjQueue];  // runs in cells whose eight labels agree
-    uint32_t mix[kMixWords][kAdjQueue];  // single samples in cells with mixed labels
+    uint32_t run[kRunWords][kAdjQueue];
     float gr[M][32];   // each lane's material weights gr_m
     float ray[9][32];  // each lane's unit ray in IJK (0-2), source in IJK (3-5), unit ray in world (6-8)
     float A[9];        // the view's IJK_from_world rotation
@@ -210,10 +208,21 @@ __device__ __forceinline__ void scatter_cell(float *grad, int i0, int j0, int k0
     }
 }
 
+// Fixed point of the texture unit for density coordinate p + 0.5 on an axis of n texels
+// (drr_texweights.h). `hw_fix_live` omits the upper clamp, which no marched sample reaches: live
+// samples satisfy p <= n - 1.5 (up to rounding), so 256 (p + 0.5) - 127.5 stays 128 below 256 (n - 1).
+__device__ __forceinline__ int hw_fix(float p, int n) {
+    return hw_fix_from_floor(__float2int_rd(__fmaf_rn(__fadd_rn(p, 0.5f), 256.0f, -127.5f)), n);
+}
+__device__ __forceinline__ int hw_fix_live(float p) {
+    return max(__float2int_rd(__fmaf_rn(__fadd_rn(p, 0.5f), 256.0f, -127.5f)), 0);
+}
+
 // Density and pose gradients of one view per blockIdx.z, one ray per thread (16 x 8 pixel tiles,
-// each warp 8 x 4 pixels). A run is a stretch of a ray's samples with one label cell, one
-// texture-filter cell and one trapezoid weight; see the file comment. 5 blocks per SM (96
-// registers) balances occupancy against the registers the drain needs.
+// each warp 8 x 4 pixels). A run is a stretch of a ray's full-weight samples with one label cell
+// and one texture-filter cell; the trapezoid half-weight samples (t = 0 and t = num_steps - 1) are
+// runs of their own. See the file comment. 5 blocks per SM (96 registers) balances occupancy
+// against the registers the drain needs.
 template <int M>
 __global__ void __launch_bounds__(kBlockThreads, 5) adjoint_kernel(const __grid_constant__ AdjointParams P) {
     __shared__ AdjointWarpSmem<M> smem[kBlockThreads / 32];
@@ -231,9 +240,9 @@ __global__ void __launch_bounds__(kBlockThreads, 5) adjoint_kernel(const __grid_
     const unsigned kAll = 0xffffffffu;
 
     AdjointRay<M> R{};
-    bool live = u < p.width && v < p.height && adjoint_setup<M>(P, av, u, v, zv, R);
+    const bool ray_live = u < p.width && v < p.height && adjoint_setup<M>(P, av, u, v, zv, R);
 #pragma unroll
-    for (int m = 0; m < M; m++) sh.gr[m][lane] = live ? R.gr[m] : 0.0f;
+    for (int m = 0; m < M; m++) sh.gr[m][lane] = ray_live ? R.gr[m] : 0.0f;
     sh.ray[0][lane] = R.rxi;
     sh.ray[1][lane] = R.ryi;
     sh.ray[2][lane] = R.rzi;
@@ -263,108 +272,16 @@ __global__ void __launch_bounds__(kBlockThreads, 5) adjoint_kernel(const __grid_
         Cs2 += ox * ky - oy * kx;
     };
 
-    // Drains `count` (<= 32) queued uniform-label runs starting at ring slot `first`, one run per
-    // lane. Each run is re-derived from its first alpha with the march's own float32 operations, so
-    // its positions, label cell and filter cell are the march's.
-    auto drain_runs = [&](int first, int count) {
-        if (lane >= count) return;
-        const int e = (first + lane) & (kAdjQueue - 1);
-        const float al = __uint_as_float(sh.run[0][e]);
-        const uint32_t w1 = sh.run[1][e];
-        const int kn = (int)(w1 & 255u), owner = (int)((w1 >> 8) & 31u);
-        const float wrun = (w1 >> 13) & 1u ? 0.5f : 1.0f;
-        const uint32_t word = sh.run[2][e];
-        const float rxi = sh.ray[0][owner], ryi = sh.ray[1][owner], rzi = sh.ray[2][owner];
-        const float sx = sh.ray[3][owner], sy = sh.ray[4][owner], sz = sh.ray[5][owner];
-        const float px = __fsub_rn(__fmaf_rn(al, rxi, sx), 1.0f);
-        const float py = __fsub_rn(__fmaf_rn(al, ryi, sy), 1.0f);
-        const float pz = __fsub_rn(__fmaf_rn(al, rzi, sz), 1.0f);
-        const float bx = floorf(px), by = floorf(py), bz = floorf(pz);
-        const int fxi = hw_fix_from_floor(__float2int_rd(__fmaf_rn(__fadd_rn(px, 0.5f), 256.0f, -127.5f)), n0);
-        const int fyi = hw_fix_from_floor(__float2int_rd(__fmaf_rn(__fadd_rn(py, 0.5f), 256.0f, -127.5f)), n1);
-        const int fzi = hw_fix_from_floor(__float2int_rd(__fmaf_rn(__fadd_rn(pz, 0.5f), 256.0f, -127.5f)), n2);
-        float h[3], hk[3];
-        float r8[8];
-        if (do_pose) {
-#pragma unroll
-            for (int c = 0; c < 8; c++)
-                r8[c] = tex3D<float>(P.density_point, bx + (float)(c & 1) + 0.5f, by + (float)((c >> 1) & 1) + 0.5f,
-                                     bz + (float)(c >> 2) + 0.5f);
-        }
-        const float gu = sh.gr[word & 15u][owner];
-        if (do_dens) {
-            // every sample of the run adds w_t gu W_c / 256 to texel c: the packed sums hold sum W_c
-            const float rv = __fmul_rn(__fmul_rn(wrun, gu), 1.0f / 256.0f);
-            float vals[8];
-#pragma unroll
-            for (int row = 0; row < 4; row++) {
-                // packed word of (dx, dy) holds dz = 0 | dz = 1 << 16
-                const int dy = row & 1, dz = row >> 1;
-                const uint32_t s0 = sh.run[3 + dy][e], s1 = sh.run[5 + dy][e];
-                vals[2 * row] = rv * (float)((s0 >> (16 * dz)) & 0xFFFFu);
-                vals[2 * row + 1] = rv * (float)((s1 >> (16 * dz)) & 0xFFFFu);
-            }
-            scatter_cell(grad, fxi >> 8, fyi >> 8, fzi >> 8, n0, n1, n2, vals);
-        }
-        if (do_pose) {
-            // grad rho = c0 + c1 f_a + c2 f_b + c3 f_a f_b per axis (f_a, f_b the other two
-            // fractions), summed over the run's samples f0 + k d, alpha0 + k delta in closed form
-            const float ax = __fsub_rn(px, bx), ay = __fsub_rn(py, by), az = __fsub_rn(pz, bz);
-            const float delta = __fsub_rn(__fadd_rn(al, step), al);  // the float32 step at alpha0
-            const float bxs = delta * rxi, bys = delta * ryi, bzs = delta * rzi;
-            const float ex = r8[1] - r8[0], ey = r8[2] - r8[0], ez = r8[4] - r8[0];
-            const float x1 = (r8[3] - r8[2]) - ex, x2 = (r8[5] - r8[4]) - ex;
-            const float x3 = (r8[7] - r8[6]) - (r8[5] - r8[4]) - (r8[3] - r8[2]) + ex;
-            const float y1 = (r8[3] - r8[1]) - ey, y2 = (r8[6] - r8[4]) - ey;
-            const float y3 = (r8[7] - r8[5]) - (r8[6] - r8[4]) - (r8[3] - r8[1]) + ey;
-            const float z1 = (r8[5] - r8[1]) - ez, z2 = (r8[6] - r8[2]) - ez;
-            const float z3 = (r8[7] - r8[3]) - (r8[6] - r8[2]) - (r8[5] - r8[1]) + ez;
-            const float kf = (float)kn;
-            const float T1 = 0.5f * kf * (kf - 1.0f);                   // sum k
-            const float T2 = T1 * (2.0f * kf - 1.0f) * (1.0f / 3.0f);  // sum k^2
-            const float T3 = T1 * T1;                                   // sum k^3
-            // moment of g: m = sum g(f_k), n = sum alpha_k g(f_k) = alpha0 m + delta sum k g(f_k)
-            float m = kf, n = al * kf + delta * T1;  // g = 1
-            h[0] = ex * m, h[1] = ey * m, h[2] = ez * m;
-            hk[0] = ex * n, hk[1] = ey * n, hk[2] = ez * n;
-            m = kf * ax + bxs * T1, n = al * m + delta * (ax * T1 + bxs * T2);  // g = f_x
-            h[1] += y1 * m, h[2] += z1 * m, hk[1] += y1 * n, hk[2] += z1 * n;
-            m = kf * ay + bys * T1, n = al * m + delta * (ay * T1 + bys * T2);  // g = f_y
-            h[0] += x1 * m, h[2] += z2 * m, hk[0] += x1 * n, hk[2] += z2 * n;
-            m = kf * az + bzs * T1, n = al * m + delta * (az * T1 + bzs * T2);  // g = f_z
-            h[0] += x2 * m, h[1] += y2 * m, hk[0] += x2 * n, hk[1] += y2 * n;
-            float c0 = ax * ay, c1 = ax * bys + ay * bxs, c2 = bxs * bys;  // g = f_x f_y
-            m = kf * c0 + c1 * T1 + c2 * T2, n = al * m + delta * (c0 * T1 + c1 * T2 + c2 * T3);
-            h[2] += z3 * m, hk[2] += z3 * n;
-            c0 = ax * az, c1 = ax * bzs + az * bxs, c2 = bxs * bzs;  // g = f_x f_z
-            m = kf * c0 + c1 * T1 + c2 * T2, n = al * m + delta * (c0 * T1 + c1 * T2 + c2 * T3);
-            h[1] += y3 * m, hk[1] += y3 * n;
-            c0 = ay * az, c1 = ay * bzs + az * bys, c2 = bys * bzs;  // g = f_y f_z
-            m = kf * c0 + c1 * T1 + c2 * T2, n = al * m + delta * (c0 * T1 + c1 * T2 + c2 * T3);
-            h[0] += x3 * m, hk[0] += x3 * n;
-            const float gw = gu * wrun;
-#pragma unroll
-            for (int c = 0; c < 3; c++) h[c] *= gw, hk[c] *= gw;
-        }
-        if (do_pose) add_pose(h, hk, owner);
-    };
-
-    // Drains `count` (<= 32) queued mixed-label samples starting at ring slot `first`, one per lane:
-    // the forward's label weights q_t, the texture unit's corner weights for the density, and the
-    // trilinear gradient of rho Q for the pose.
-    auto drain_mixed = [&](int first, int count) {
-        if (lane >= count) return;
-        const int e = (first + lane) & (kAdjQueue - 1);
-        const float al = __uint_as_float(sh.mix[0][e]);
-        const uint32_t w1 = sh.mix[1][e];
-        const int owner = (int)((w1 >> 8) & 31u);
-        const float wrun = (w1 >> 13) & 1u ? 0.5f : 1.0f;
-        const uint32_t word = sh.mix[2][e];
+    // One sample of a mixed-label cell at float32 alpha `al` of ray `owner`: the forward's label
+    // weights q_t with the texture unit's corner weights for the density, the trilinear gradient of
+    // rho Q for the pose.
+    auto mixed_sample = [&](float al, int owner, float wrun) {
         const float px = __fsub_rn(__fmaf_rn(al, sh.ray[0][owner], sh.ray[3][owner]), 1.0f);
         const float py = __fsub_rn(__fmaf_rn(al, sh.ray[1][owner], sh.ray[4][owner]), 1.0f);
         const float pz = __fsub_rn(__fmaf_rn(al, sh.ray[2][owner], sh.ray[5][owner]), 1.0f);
         const float bx = floorf(px), by = floorf(py), bz = floorf(pz);
         const float fx = __fsub_rn(px, bx), fy = __fsub_rn(py, by), fz = __fsub_rn(pz, bz);
+        const uint32_t word = fetch_label_word(V, bx, by, bz);
         float g8[8];
 #pragma unroll
         for (int c = 0; c < 8; c++) g8[c] = sh.gr[(word >> (4 * c)) & 15u][owner];
@@ -374,9 +291,7 @@ __global__ void __launch_bounds__(kBlockThreads, 5) adjoint_kernel(const __grid_
 #pragma unroll
             for (int c = 0; c < 8; c++) q = __fmaf_rn(__fmul_rn(cw.xy[c & 3], cw.z[c >> 2]), g8[c], q);
             const float rv = __fmul_rn(__fmul_rn(wrun, q), 1.0f / 256.0f);
-            const int fxi = hw_fix_from_floor(__float2int_rd(__fmaf_rn(__fadd_rn(px, 0.5f), 256.0f, -127.5f)), n0);
-            const int fyi = hw_fix_from_floor(__float2int_rd(__fmaf_rn(__fadd_rn(py, 0.5f), 256.0f, -127.5f)), n1);
-            const int fzi = hw_fix_from_floor(__float2int_rd(__fmaf_rn(__fadd_rn(pz, 0.5f), 256.0f, -127.5f)), n2);
+            const int fxi = hw_fix(px, n0), fyi = hw_fix(py, n1), fzi = hw_fix(pz, n2);
             int W[8];
             hw_corner_weights(fxi & 255, fyi & 255, fzi & 255, W);
             float vals[8];
@@ -406,85 +321,216 @@ __global__ void __launch_bounds__(kBlockThreads, 5) adjoint_kernel(const __grid_
         }
     };
 
+    // Drains `count` (<= 32) queued runs starting at ring slot `first`, one run per lane. Each run is
+    // re-derived from its first alpha with the march's own float32 operations, so its positions,
+    // label cell and filter cell are the march's. Runs in cells with mixed labels are then split
+    // into their samples, which the warp evaluates 32 at a time.
+    auto drain = [&](int first, int count) {
+        const bool mine = lane < count;
+        const int e = (first + lane) & (kAdjQueue - 1);
+        float al = 0.0f, wrun = 1.0f;
+        int kn = 0, owner = 0;
+        bool mixed = false;
+        if (mine) {
+            al = __uint_as_float(sh.run[0][e]);
+            const uint32_t w1 = sh.run[1][e];
+            kn = (int)(w1 & 255u), owner = (int)((w1 >> 8) & 31u);
+            wrun = (w1 >> 13) & 1u ? 0.5f : 1.0f;
+            const float rxi = sh.ray[0][owner], ryi = sh.ray[1][owner], rzi = sh.ray[2][owner];
+            const float px = __fsub_rn(__fmaf_rn(al, rxi, sh.ray[3][owner]), 1.0f);
+            const float py = __fsub_rn(__fmaf_rn(al, ryi, sh.ray[4][owner]), 1.0f);
+            const float pz = __fsub_rn(__fmaf_rn(al, rzi, sh.ray[5][owner]), 1.0f);
+            const float bx = floorf(px), by = floorf(py), bz = floorf(pz);
+            const uint32_t word = fetch_label_word(V, bx, by, bz);
+            mixed = !uniform_word(word);
+            float r8[8];
+            if (do_pose && !mixed) {
+#pragma unroll
+                for (int c = 0; c < 8; c++)
+                    r8[c] = tex3D<float>(P.density_point, bx + (float)(c & 1) + 0.5f,
+                                         by + (float)((c >> 1) & 1) + 0.5f, bz + (float)(c >> 2) + 0.5f);
+            }
+            if (!mixed) {
+                const float gu = sh.gr[word & 15u][owner];
+                if (do_dens) {
+                    // every sample adds w_t gu W_c / 256 to texel c: the packed sums hold sum W_c
+                    const float rv = __fmul_rn(__fmul_rn(wrun, gu), 1.0f / 256.0f);
+                    float vals[8];
+#pragma unroll
+                    for (int row = 0; row < 4; row++) {
+                        // packed word of (dx, dy) holds dz = 0 | dz = 1 << 16
+                        const int dy = row & 1, dz = row >> 1;
+                        const uint32_t s0 = sh.run[2 + dy][e], s1 = sh.run[4 + dy][e];
+                        vals[2 * row] = rv * (float)((s0 >> (16 * dz)) & 0xFFFFu);
+                        vals[2 * row + 1] = rv * (float)((s1 >> (16 * dz)) & 0xFFFFu);
+                    }
+                    scatter_cell(grad, hw_fix(px, n0) >> 8, hw_fix(py, n1) >> 8, hw_fix(pz, n2) >> 8, n0, n1, n2,
+                                 vals);
+                }
+                if (do_pose) {
+                    // grad rho = c0 + c1 f_a + c2 f_b + c3 f_a f_b per axis (f_a, f_b the other two
+                    // fractions), summed over the run's samples f0 + k d, alpha0 + k delta in closed form
+                    const float ax = __fsub_rn(px, bx), ay = __fsub_rn(py, by), az = __fsub_rn(pz, bz);
+                    const float delta = __fsub_rn(__fadd_rn(al, step), al);  // the float32 step at alpha0
+                    const float bxs = delta * rxi, bys = delta * ryi, bzs = delta * rzi;
+                    const float ex = r8[1] - r8[0], ey = r8[2] - r8[0], ez = r8[4] - r8[0];
+                    const float x1 = (r8[3] - r8[2]) - ex, x2 = (r8[5] - r8[4]) - ex;
+                    const float x3 = (r8[7] - r8[6]) - (r8[5] - r8[4]) - (r8[3] - r8[2]) + ex;
+                    const float y1 = (r8[3] - r8[1]) - ey, y2 = (r8[6] - r8[4]) - ey;
+                    const float y3 = (r8[7] - r8[5]) - (r8[6] - r8[4]) - (r8[3] - r8[1]) + ey;
+                    const float z1 = (r8[5] - r8[1]) - ez, z2 = (r8[6] - r8[2]) - ez;
+                    const float z3 = (r8[7] - r8[3]) - (r8[6] - r8[2]) - (r8[5] - r8[1]) + ez;
+                    const float kf = (float)kn;
+                    const float T1 = 0.5f * kf * (kf - 1.0f);                   // sum k
+                    const float T2 = T1 * (2.0f * kf - 1.0f) * (1.0f / 3.0f);  // sum k^2
+                    const float T3 = T1 * T1;                                   // sum k^3
+                    // moment of g: m = sum g(f_k), n = sum alpha_k g(f_k) = alpha0 m + delta sum k g(f_k)
+                    float h[3], hk[3];
+                    float m = kf, n = al * kf + delta * T1;  // g = 1
+                    h[0] = ex * m, h[1] = ey * m, h[2] = ez * m;
+                    hk[0] = ex * n, hk[1] = ey * n, hk[2] = ez * n;
+                    m = kf * ax + bxs * T1, n = al * m + delta * (ax * T1 + bxs * T2);  // g = f_x
+                    h[1] += y1 * m, h[2] += z1 * m, hk[1] += y1 * n, hk[2] += z1 * n;
+                    m = kf * ay + bys * T1, n = al * m + delta * (ay * T1 + bys * T2);  // g = f_y
+                    h[0] += x1 * m, h[2] += z2 * m, hk[0] += x1 * n, hk[2] += z2 * n;
+                    m = kf * az + bzs * T1, n = al * m + delta * (az * T1 + bzs * T2);  // g = f_z
+                    h[0] += x2 * m, h[1] += y2 * m, hk[0] += x2 * n, hk[1] += y2 * n;
+                    float c0 = ax * ay, c1 = ax * bys + ay * bxs, c2 = bxs * bys;  // g = f_x f_y
+                    m = kf * c0 + c1 * T1 + c2 * T2, n = al * m + delta * (c0 * T1 + c1 * T2 + c2 * T3);
+                    h[2] += z3 * m, hk[2] += z3 * n;
+                    c0 = ax * az, c1 = ax * bzs + az * bxs, c2 = bxs * bzs;  // g = f_x f_z
+                    m = kf * c0 + c1 * T1 + c2 * T2, n = al * m + delta * (c0 * T1 + c1 * T2 + c2 * T3);
+                    h[1] += y3 * m, hk[1] += y3 * n;
+                    c0 = ay * az, c1 = ay * bzs + az * bys, c2 = bys * bzs;  // g = f_y f_z
+                    m = kf * c0 + c1 * T1 + c2 * T2, n = al * m + delta * (c0 * T1 + c1 * T2 + c2 * T3);
+                    h[0] += x3 * m, hk[0] += x3 * n;
+                    const float gw = gu * wrun;
+#pragma unroll
+                    for (int c = 0; c < 3; c++) h[c] *= gw, hk[c] *= gw;
+                    add_pose(h, hk, owner);
+                }
+            }
+        }
+        // mixed-label runs: their samples, numbered across the warp, 32 at a time
+        int nmix = mixed ? kn : 0;
+        int off = nmix;  // inclusive prefix sum over the lanes
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int x = __shfl_up_sync(kAll, off, o);
+            if (lane >= o) off += x;
+        }
+        const int total = __shfl_sync(kAll, off, 31);
+        for (int base = 0; base < total; base += 32) {
+            const int g = base + lane;
+            // the run holding sample g: the first lane whose inclusive prefix exceeds g
+            int src = 0;
+#pragma unroll
+            for (int b = 16; b > 0; b >>= 1) {
+                const int cand = src + b;
+                const int o_c = __shfl_sync(kAll, off, cand - 1);
+                if (o_c <= g) src = cand;
+            }
+            // every lane takes part in every shuffle (lane src - 1 wraps to 31 for src = 0)
+            const int o_before = __shfl_sync(kAll, off, (src + 31) & 31);
+            const int o_prev = src > 0 ? o_before : 0;
+            const float s_al = __shfl_sync(kAll, al, src);
+            const int s_owner = __shfl_sync(kAll, owner, src) & 31;
+            const float s_w = __shfl_sync(kAll, wrun, src);
+            if (g < total) {
+                float a = s_al;
+                // exactly g - o_prev (< 255) additions from the run's first alpha
+                advance_alpha(&a, step, __int_as_float(0x7f800000), min(max(g - o_prev, 0), 254), false);
+                mixed_sample(a, s_owner, s_w);
+            }
+        }
+    };
+
+    // Phases of each ray: [a half-weight sample at t = 0] [full-weight samples] [a half-weight
+    // sample at t = num_steps - 1], each phase for the whole warp at once.
     float alpha = R.alpha;
     int t = R.t;
-    const int t_end = R.t_end, t_last = R.num_steps - 1;
-    // the current sample: position, label cell and label word (the next word is loaded a step ahead)
-    float cx = 0.0f, cy = 0.0f, cz = 0.0f, cbx = 0.0f, cby = 0.0f, cbz = 0.0f;
-    uint32_t w_cur = 0;
+    const bool first_half = ray_live && R.t == 0;
+    const bool last_half = ray_live && R.t_end == R.num_steps && R.num_steps > 1;
+    const int t_stop = last_half ? R.num_steps - 1 : R.t_end;  // end of the full-weight samples
+    int head = 0, queued = 0;  // warp-uniform ring state
+    const unsigned lt = (1u << lane) - 1u;
+
+    // the open run: sample count, first alpha, label cell, filter fixed point, packed sums
+    int K = 0;
+    float a0 = 0.0f, rbx = 0.0f, rby = 0.0f, rbz = 0.0f;
+    int rfx = 0, rfy = 0, rfz = 0;
+    uint32_t S0 = 0, S1 = 0, S2 = 0, S3 = 0;
+
+    auto enqueue = [&](bool push, bool half) {
+        const unsigned pm = __ballot_sync(kAll, push);
+        if (push) {
+            const int s = (head + queued + __popc(pm & lt)) & (kAdjQueue - 1);
+            sh.run[0][s] = __float_as_uint(a0);
+            sh.run[1][s] = (uint32_t)K | ((uint32_t)lane << 8) | (half ? 1u << 13 : 0u);
+            sh.run[2][s] = S0;
+            sh.run[3][s] = S1;
+            sh.run[4][s] = S2;
+            sh.run[5][s] = S3;
+            K = 0;
+        }
+        queued += __popc(pm);
+        if (queued >= 32) {
+            __syncwarp();
+            drain(head, 32);
+            __syncwarp();
+            head = (head + 32) & (kAdjQueue - 1);
+            queued -= 32;
+        }
+    };
+    // a single-sample run at the current alpha (the half-weight samples)
+    auto single = [&](bool here) {
+        if (here) {
+            const float cx = __fsub_rn(__fmaf_rn(alpha, R.rxi, R.sx), 1.0f);
+            const float cy = __fsub_rn(__fmaf_rn(alpha, R.ryi, R.sy), 1.0f);
+            const float cz = __fsub_rn(__fmaf_rn(alpha, R.rzi, R.sz), 1.0f);
+            uint32_t Wp[4] = {0u, 0u, 0u, 0u};
+            if (do_dens) {
+                const int fxi = hw_fix(cx, n0), fyi = hw_fix(cy, n1), fzi = hw_fix(cz, n2);
+                packed_corner_weights((uint32_t)fxi & 255u, (uint32_t)fyi & 255u, (uint32_t)fzi & 255u, Wp);
+            }
+            a0 = alpha;
+            K = 1;
+            S0 = Wp[0], S1 = Wp[1], S2 = Wp[2], S3 = Wp[3];
+        }
+        enqueue(here, true);
+    };
+
+    single(first_half);
+    if (first_half) {
+        alpha = __fadd_rn(alpha, step);
+        ++t;
+    }
+    bool live = t < t_stop;
+    float cx = 0.0f, cy = 0.0f, cz = 0.0f;
     if (live) {
         cx = __fsub_rn(__fmaf_rn(alpha, R.rxi, R.sx), 1.0f);
         cy = __fsub_rn(__fmaf_rn(alpha, R.ryi, R.sy), 1.0f);
         cz = __fsub_rn(__fmaf_rn(alpha, R.rzi, R.sz), 1.0f);
-        cbx = floorf(cx), cby = floorf(cy), cbz = floorf(cz);
-        w_cur = fetch_label_word(V, cbx, cby, cbz);
     }
-    // the open run: sample count, first alpha, label cell, filter fixed point, weight, packed sums
-    int K = 0;
-    float a0 = 0.0f, rbx = 0.0f, rby = 0.0f, rbz = 0.0f, rw = 0.0f;
-    int rfx = 0, rfy = 0, rfz = 0;
-    uint32_t rword = 0, S0 = 0, S1 = 0, S2 = 0, S3 = 0;
-    bool rmixed = false;       // the open run is one sample of a mixed-label cell
-    int head = 0, queued = 0;  // warp-uniform ring state of the uniform-label runs
-    int mhead = 0, mqueued = 0;  // and of the mixed-label samples
-    const unsigned lt = (1u << lane) - 1u;
-
-    for (;;) {
-        const bool have = live;
+    while (__any_sync(kAll, live || K > 0)) {
         bool fresh = false;
         int fxi = 0, fyi = 0, fzi = 0;
-        float wt = 1.0f, an = 0.0f, nx = 0.0f, ny = 0.0f, nz = 0.0f, nbx = 0.0f, nby = 0.0f, nbz = 0.0f;
-        uint32_t w_next = 0;
-        if (have) {
-            an = __fadd_rn(alpha, step);
-            nx = __fsub_rn(__fmaf_rn(an, R.rxi, R.sx), 1.0f);
-            ny = __fsub_rn(__fmaf_rn(an, R.ryi, R.sy), 1.0f);
-            nz = __fsub_rn(__fmaf_rn(an, R.rzi, R.sz), 1.0f);
-            nbx = floorf(nx), nby = floorf(ny), nbz = floorf(nz);
-            w_next = fetch_label_word(V, nbx, nby, nbz);
-            wt = (0 == t || t_last == t) ? 0.5f : 1.0f;
-            fresh = K == 0 || K == 255 || rmixed || cbx != rbx || cby != rby || cbz != rbz || wt != rw;
+        float bx = 0.0f, by = 0.0f, bz = 0.0f;
+        if (live) {
+            bx = floorf(cx), by = floorf(cy), bz = floorf(cz);
+            fresh = K == 0 || K == 255 || bx != rbx || by != rby || bz != rbz;
             if (do_dens) {
-                // texture-unit fixed point of the density coordinate p + 0.5 (drr_texweights.h)
-                fxi = hw_fix_from_floor(__float2int_rd(__fmaf_rn(__fadd_rn(cx, 0.5f), 256.0f, -127.5f)), n0);
-                fyi = hw_fix_from_floor(__float2int_rd(__fmaf_rn(__fadd_rn(cy, 0.5f), 256.0f, -127.5f)), n1);
-                fzi = hw_fix_from_floor(__float2int_rd(__fmaf_rn(__fadd_rn(cz, 0.5f), 256.0f, -127.5f)), n2);
+                fxi = hw_fix_live(cx), fyi = hw_fix_live(cy), fzi = hw_fix_live(cz);
                 fresh = fresh || ((fxi ^ rfx) | (fyi ^ rfy) | (fzi ^ rfz)) >= 256;
             }
         }
-        // a run ends when the next sample starts a new one or the ray has no samples left
-        const bool push = K > 0 && (!have || fresh);
-        const unsigned pm = __ballot_sync(kAll, push && !rmixed);
-        const unsigned mm = __ballot_sync(kAll, push && rmixed);
-        if (push) {
-            const uint32_t tag = ((uint32_t)lane << 8) | (rw != 1.0f ? 1u << 13 : 0u);
-            if (!rmixed) {
-                const int s = (head + queued + __popc(pm & lt)) & (kAdjQueue - 1);
-                sh.run[0][s] = __float_as_uint(a0);
-                sh.run[1][s] = (uint32_t)K | tag;
-                sh.run[2][s] = rword;
-                sh.run[3][s] = S0;
-                sh.run[4][s] = S1;
-                sh.run[5][s] = S2;
-                sh.run[6][s] = S3;
-            } else {
-                const int s = (mhead + mqueued + __popc(mm & lt)) & (kAdjQueue - 1);
-                sh.mix[0][s] = __float_as_uint(a0);
-                sh.mix[1][s] = tag;
-                sh.mix[2][s] = rword;
-            }
-            K = 0;
-        }
-        queued += __popc(pm);
-        mqueued += __popc(mm);
-        if (have) {
+        // a run ends when this sample starts a new one or the ray has no full-weight samples left
+        enqueue(K > 0 && (!live || fresh), false);
+        if (live) {
             if (K == 0) {
                 a0 = alpha;
-                rbx = cbx, rby = cby, rbz = cbz;
+                rbx = bx, rby = by, rbz = bz;
                 rfx = fxi, rfy = fyi, rfz = fzi;
-                rw = wt;
-                rword = w_cur;
-                rmixed = !uniform_word(w_cur);
                 S0 = S1 = S2 = S3 = 0u;
             }
             if (do_dens) {
@@ -494,30 +540,16 @@ __global__ void __launch_bounds__(kBlockThreads, 5) adjoint_kernel(const __grid_
             }
             ++K;
             ++t;
-            alpha = an;
-            cx = nx, cy = ny, cz = nz, cbx = nbx, cby = nby, cbz = nbz;
-            w_cur = w_next;
-            live = t < t_end;
+            alpha = __fadd_rn(alpha, step);
+            cx = __fsub_rn(__fmaf_rn(alpha, R.rxi, R.sx), 1.0f);
+            cy = __fsub_rn(__fmaf_rn(alpha, R.ryi, R.sy), 1.0f);
+            cz = __fsub_rn(__fmaf_rn(alpha, R.rzi, R.sz), 1.0f);
+            live = t < t_stop;
         }
-        if (queued >= 32) {
-            __syncwarp();
-            drain_runs(head, 32);
-            __syncwarp();
-            head = (head + 32) & (kAdjQueue - 1);
-            queued -= 32;
-        }
-        if (mqueued >= 32) {
-            __syncwarp();
-            drain_mixed(mhead, 32);
-            __syncwarp();
-            mhead = (mhead + 32) & (kAdjQueue - 1);
-            mqueued -= 32;
-        }
-        if (!__any_sync(kAll, live || K > 0)) break;
     }
+    single(last_half);
     __syncwarp();
-    drain_runs(head, queued);
-    drain_mixed(mhead, mqueued);
+    drain(head, queued);
 
     if (do_pose) {
         // the warp's pose sums: one atomic per component
