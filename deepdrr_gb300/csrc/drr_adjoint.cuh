@@ -177,6 +177,7 @@ struct AdjointWarpSmem {
     uint32_t run[kRunWords][kAdjQueue];
     float gr[M][32];   // each lane's material weights gr_m
     float ray[9][32];  // each lane's unit ray in IJK (0-2), source in IJK (3-5), unit ray in world (6-8)
+    float pose[6][32];  // each lane's share of the drained pose sums: h (IJK, 0-2), r x A^T hk (3-5)
     float A[9];        // the view's IJK_from_world rotation
 };
 
@@ -258,18 +259,19 @@ __global__ void __launch_bounds__(kBlockThreads, 5) adjoint_kernel(const __grid_
     const int n0 = V.n[0], n1 = V.n[1], n2 = V.n[2];
     const float step = p.step;
     float *const grad = P.grad_density;
-    float Hs0 = 0.0f, Hs1 = 0.0f, Hs2 = 0.0f, Cs0 = 0.0f, Cs1 = 0.0f, Cs2 = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 6; k++) sh.pose[k][lane] = 0.0f;
 
-    // r_owner x (A^T hk) in world coordinates, and the IJK sum h, into this lane's pose sums
+    // the IJK sum h and r_owner x (A^T hk) in world coordinates, into this lane's pose sums
     auto add_pose = [&](const float h[3], const float hk[3], int owner) {
-        Hs0 += h[0], Hs1 += h[1], Hs2 += h[2];
+        sh.pose[0][lane] += h[0], sh.pose[1][lane] += h[1], sh.pose[2][lane] += h[2];
         const float kx = sh.A[0] * hk[0] + sh.A[3] * hk[1] + sh.A[6] * hk[2];
         const float ky = sh.A[1] * hk[0] + sh.A[4] * hk[1] + sh.A[7] * hk[2];
         const float kz = sh.A[2] * hk[0] + sh.A[5] * hk[1] + sh.A[8] * hk[2];
         const float ox = sh.ray[6][owner], oy = sh.ray[7][owner], oz = sh.ray[8][owner];
-        Cs0 += oy * kz - oz * ky;
-        Cs1 += oz * kx - ox * kz;
-        Cs2 += ox * ky - oy * kx;
+        sh.pose[3][lane] += oy * kz - oz * ky;
+        sh.pose[4][lane] += oz * kx - ox * kz;
+        sh.pose[5][lane] += ox * ky - oy * kx;
     };
 
     // One sample of a mixed-label cell at float32 alpha `al` of ray `owner`: the forward's label
@@ -553,6 +555,8 @@ __global__ void __launch_bounds__(kBlockThreads, 5) adjoint_kernel(const __grid_
 
     if (do_pose) {
         // the warp's pose sums: one atomic per component
+        float Hs0 = sh.pose[0][lane], Hs1 = sh.pose[1][lane], Hs2 = sh.pose[2][lane];
+        float Cs0 = sh.pose[3][lane], Cs1 = sh.pose[4][lane], Cs2 = sh.pose[5][lane];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             Hs0 += __shfl_xor_sync(kAll, Hs0, o);
