@@ -171,10 +171,12 @@ __device__ __forceinline__ bool adjoint_setup(const AdjointParams &P, const Adjo
 // of entry e at [k][e]); the warp drains 32 runs at a time.
 constexpr int kAdjQueue = 64;
 constexpr int kRunWords = 6;  // alpha0, count | lane << 8 | half << 13, four packed corner sums
+constexpr int kMixWords = 3;  // alpha0, count | lane << 8 | half << 13, label word
 
 template <int M>
 struct AdjointWarpSmem {
     uint32_t run[kRunWords][kAdjQueue];
+    uint32_t mix[kMixWords][kAdjQueue];  // runs in cells with mixed labels, set aside by the drain
     float gr[M][32];   // each lane's material weights gr_m
     float ray[9][32];  // each lane's unit ray in IJK (0-2), source in IJK (3-5), unit ray in world (6-8)
     float pose[6][32];  // each lane's share of the drained pose sums: h (IJK, 0-2), r x A^T hk (3-5)
@@ -217,6 +219,128 @@ __device__ __forceinline__ int hw_fix(float p, int n) {
 }
 __device__ __forceinline__ int hw_fix_live(float p) {
     return max(__float2int_rd(__fmaf_rn(__fadd_rn(p, 0.5f), 256.0f, -127.5f)), 0);
+}
+
+// The IJK sum h and r_owner x (A^T hk) in world coordinates, into lane `lane`'s pose sums.
+template <int M>
+__device__ __forceinline__ void add_pose_sums(AdjointWarpSmem<M> &sh, int lane, const float h[3], const float hk[3],
+                                              int owner) {
+    sh.pose[0][lane] += h[0], sh.pose[1][lane] += h[1], sh.pose[2][lane] += h[2];
+    const float kx = sh.A[0] * hk[0] + sh.A[3] * hk[1] + sh.A[6] * hk[2];
+    const float ky = sh.A[1] * hk[0] + sh.A[4] * hk[1] + sh.A[7] * hk[2];
+    const float kz = sh.A[2] * hk[0] + sh.A[5] * hk[1] + sh.A[8] * hk[2];
+    const float ox = sh.ray[6][owner], oy = sh.ray[7][owner], oz = sh.ray[8][owner];
+    sh.pose[3][lane] += oy * kz - oz * ky;
+    sh.pose[4][lane] += oz * kx - ox * kz;
+    sh.pose[5][lane] += ox * ky - oy * kx;
+}
+
+// One sample of a mixed-label cell at float32 alpha `al` of ray `owner` (label word `word`): the
+// forward's label weights q_t with the texture unit's corner weights for the density, the
+// trilinear gradient of rho Q for the pose. Written corner by corner so that few registers stay
+// live: it runs rarely, inside the march's register budget.
+template <int M>
+__device__ __forceinline__ void mixed_sample(const AdjointParams &P, AdjointWarpSmem<M> &sh, int lane, float al,
+                                             int owner, float wrun, uint32_t word) {
+    const VolConst &V = P.s.vol[0];
+    const int n0 = V.n[0], n1 = V.n[1], n2 = V.n[2];
+    const float px = __fsub_rn(__fmaf_rn(al, sh.ray[0][owner], sh.ray[3][owner]), 1.0f);
+    const float py = __fsub_rn(__fmaf_rn(al, sh.ray[1][owner], sh.ray[4][owner]), 1.0f);
+    const float pz = __fsub_rn(__fmaf_rn(al, sh.ray[2][owner], sh.ray[5][owner]), 1.0f);
+    const float bx = floorf(px), by = floorf(py), bz = floorf(pz);
+    const float fx = __fsub_rn(px, bx), fy = __fsub_rn(py, by), fz = __fsub_rn(pz, bz);
+    if (P.grad_density != nullptr) {
+        const CornerWeights cw = corner_weights(fx, fy, fz);
+        float q = 0.0f;
+#pragma unroll
+        for (int c = 0; c < 8; c++)
+            q = __fmaf_rn(__fmul_rn(cw.xy[c & 3], cw.z[c >> 2]), sh.gr[(word >> (4 * c)) & 15u][owner], q);
+        const float rv = __fmul_rn(__fmul_rn(wrun, q), 1.0f / 256.0f);
+        const int fxi = hw_fix(px, n0), fyi = hw_fix(py, n1), fzi = hw_fix(pz, n2);
+        uint32_t Wp[4];
+        packed_corner_weights((uint32_t)fxi & 255u, (uint32_t)fyi & 255u, (uint32_t)fzi & 255u, Wp);
+        const int i0 = fxi >> 8, j0 = fyi >> 8, k0 = fzi >> 8;
+        const int i1 = min(i0 + 1, n0 - 1), j1 = min(j0 + 1, n1 - 1), k1 = min(k0 + 1, n2 - 1);
+#pragma unroll 1
+        for (int c = 0; c < 8; c++) {
+            const int dx = c & 1, dy = (c >> 1) & 1, dz = c >> 2;
+            const float w = (float)((Wp[dx * 2 + dy] >> (16 * dz)) & 0xFFFFu);
+            if (w != 0.0f && rv != 0.0f)
+                atomicAdd(P.grad_density + ((size_t)(dz ? k1 : k0) * n1 + (dy ? j1 : j0)) * n0 + (dx ? i1 : i0), rv * w);
+        }
+    }
+    if (P.grad_pose != nullptr) {
+        // rho, Q and their gradients, corner by corner
+        float rho = 0.0f, Q = 0.0f, dr0 = 0.0f, dr1 = 0.0f, dr2 = 0.0f, dq0 = 0.0f, dq1 = 0.0f, dq2 = 0.0f;
+#pragma unroll 1
+        for (int c = 0; c < 8; c++) {
+            const float ox = (float)(c & 1), oy = (float)((c >> 1) & 1), oz = (float)(c >> 2);
+            const float rc = tex3D<float>(P.density_point, bx + ox + 0.5f, by + oy + 0.5f, bz + oz + 0.5f);
+            const float gc = sh.gr[(word >> (4 * c)) & 15u][owner];
+            const float wx = c & 1 ? fx : 1.0f - fx, wy = c & 2 ? fy : 1.0f - fy, wz = c & 4 ? fz : 1.0f - fz;
+            const float sx = c & 1 ? 1.0f : -1.0f, sy = c & 2 ? 1.0f : -1.0f, sz = c & 4 ? 1.0f : -1.0f;
+            const float bxy = wx * wy, bxz = wx * wz, byz = wy * wz, bc = bxy * wz;
+            rho += rc * bc, Q += gc * bc;
+            dr0 += rc * sx * byz, dr1 += rc * sy * bxz, dr2 += rc * sz * bxy;
+            dq0 += gc * sx * byz, dq1 += gc * sy * bxz, dq2 += gc * sz * bxy;
+        }
+        float h[3], hk[3];
+        h[0] = wrun * (dr0 * Q + rho * dq0), h[1] = wrun * (dr1 * Q + rho * dq1), h[2] = wrun * (dr2 * Q + rho * dq2);
+#pragma unroll
+        for (int c = 0; c < 3; c++) hk[c] = al * h[c];
+        add_pose_sums<M>(sh, lane, h, hk, owner);
+    }
+}
+
+// Drains `count` (<= 32) queued mixed-label runs starting at mixed-ring slot `first`: their
+// samples, numbered across the warp, are evaluated 32 at a time. Called by the whole warp.
+template <int M>
+__device__ __forceinline__ void drain_mixed(const AdjointParams &P, AdjointWarpSmem<M> &sh, int lane, int first,
+                                         int count) {
+    const unsigned kAll = 0xffffffffu;
+    const float step = P.s.step;
+    float al = 0.0f, wrun = 1.0f;
+    int kn = 0, owner = 0;
+    uint32_t word = 0;
+    if (lane < count) {
+        const int e = (first + lane) & (kAdjQueue - 1);
+        al = __uint_as_float(sh.mix[0][e]);
+        const uint32_t w1 = sh.mix[1][e];
+        kn = (int)(w1 & 255u), owner = (int)((w1 >> 8) & 31u);
+        wrun = (w1 >> 13) & 1u ? 0.5f : 1.0f;
+        word = sh.mix[2][e];
+    }
+    int off = kn;  // inclusive prefix sum over the lanes
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int x = __shfl_up_sync(kAll, off, o);
+        if (lane >= o) off += x;
+    }
+    const int total = __shfl_sync(kAll, off, 31);
+    for (int base = 0; base < total; base += 32) {
+        const int g = base + lane;
+        // the run holding sample g: the first lane whose inclusive prefix exceeds g
+        int src = 0;
+#pragma unroll
+        for (int b = 16; b > 0; b >>= 1) {
+            const int cand = src + b;
+            const int o_c = __shfl_sync(kAll, off, cand - 1);
+            if (o_c <= g) src = cand;
+        }
+        // every lane takes part in every shuffle (lane src - 1 wraps to 31 for src = 0)
+        const int o_before = __shfl_sync(kAll, off, (src + 31) & 31);
+        const int o_prev = src > 0 ? o_before : 0;
+        const float s_al = __shfl_sync(kAll, al, src);
+        const int s_owner = __shfl_sync(kAll, owner, src) & 31;
+        const float s_w = __shfl_sync(kAll, wrun, src);
+        const uint32_t s_word = __shfl_sync(kAll, word, src);
+        if (g < total) {
+            float a = s_al;
+            // the march's float32 alpha sequence: g - o_prev (< 255) additions from the run's first
+            for (int k = min(max(g - o_prev, 0), 254); k > 0; --k) a = __fadd_rn(a, step);
+            mixed_sample<M>(P, sh, lane, a, s_owner, s_w, s_word);
+        }
+    }
 }
 
 // Density and pose gradients of one view per blockIdx.z, one ray per thread (16 x 8 pixel tiles,
@@ -262,66 +386,11 @@ __global__ void __launch_bounds__(kBlockThreads, 5) adjoint_kernel(const __grid_
 #pragma unroll
     for (int k = 0; k < 6; k++) sh.pose[k][lane] = 0.0f;
 
-    // the IJK sum h and r_owner x (A^T hk) in world coordinates, into this lane's pose sums
-    auto add_pose = [&](const float h[3], const float hk[3], int owner) {
-        sh.pose[0][lane] += h[0], sh.pose[1][lane] += h[1], sh.pose[2][lane] += h[2];
-        const float kx = sh.A[0] * hk[0] + sh.A[3] * hk[1] + sh.A[6] * hk[2];
-        const float ky = sh.A[1] * hk[0] + sh.A[4] * hk[1] + sh.A[7] * hk[2];
-        const float kz = sh.A[2] * hk[0] + sh.A[5] * hk[1] + sh.A[8] * hk[2];
-        const float ox = sh.ray[6][owner], oy = sh.ray[7][owner], oz = sh.ray[8][owner];
-        sh.pose[3][lane] += oy * kz - oz * ky;
-        sh.pose[4][lane] += oz * kx - ox * kz;
-        sh.pose[5][lane] += ox * ky - oy * kx;
-    };
+    int head = 0, queued = 0;    // warp-uniform state of the run ring
+    int mhead = 0, mqueued = 0;  // and of the mixed-label ring
+    const unsigned lt = (1u << lane) - 1u;
 
-    // One sample of a mixed-label cell at float32 alpha `al` of ray `owner`: the forward's label
-    // weights q_t with the texture unit's corner weights for the density, the trilinear gradient of
-    // rho Q for the pose.
-    auto mixed_sample = [&](float al, int owner, float wrun) {
-        const float px = __fsub_rn(__fmaf_rn(al, sh.ray[0][owner], sh.ray[3][owner]), 1.0f);
-        const float py = __fsub_rn(__fmaf_rn(al, sh.ray[1][owner], sh.ray[4][owner]), 1.0f);
-        const float pz = __fsub_rn(__fmaf_rn(al, sh.ray[2][owner], sh.ray[5][owner]), 1.0f);
-        const float bx = floorf(px), by = floorf(py), bz = floorf(pz);
-        const float fx = __fsub_rn(px, bx), fy = __fsub_rn(py, by), fz = __fsub_rn(pz, bz);
-        const uint32_t word = fetch_label_word(V, bx, by, bz);
-        float g8[8];
-#pragma unroll
-        for (int c = 0; c < 8; c++) g8[c] = sh.gr[(word >> (4 * c)) & 15u][owner];
-        if (do_dens) {
-            const CornerWeights cw = corner_weights(fx, fy, fz);
-            float q = 0.0f;
-#pragma unroll
-            for (int c = 0; c < 8; c++) q = __fmaf_rn(__fmul_rn(cw.xy[c & 3], cw.z[c >> 2]), g8[c], q);
-            const float rv = __fmul_rn(__fmul_rn(wrun, q), 1.0f / 256.0f);
-            const int fxi = hw_fix(px, n0), fyi = hw_fix(py, n1), fzi = hw_fix(pz, n2);
-            int W[8];
-            hw_corner_weights(fxi & 255, fyi & 255, fzi & 255, W);
-            float vals[8];
-#pragma unroll
-            for (int c = 0; c < 8; c++) vals[c] = rv * (float)W[c];
-            scatter_cell(grad, fxi >> 8, fyi >> 8, fzi >> 8, n0, n1, n2, vals);
-        }
-        if (do_pose) {
-            float r8[8];
-#pragma unroll
-            for (int c = 0; c < 8; c++)
-                r8[c] = tex3D<float>(P.density_point, bx + (float)(c & 1) + 0.5f, by + (float)((c >> 1) & 1) + 0.5f,
-                                     bz + (float)(c >> 2) + 0.5f);
-            const float gx = 1.0f - fx, gy = 1.0f - fy, gz = 1.0f - fz;
-            float dr[3], dQ[3];
-            trilinear_grad(r8, fx, fy, fz, gx, gy, gz, dr);
-            trilinear_grad(g8, fx, fy, fz, gx, gy, gz, dQ);
-            const float rho = trilinear(r8, fx, fy, fz, gx, gy, gz);
-            const float Q = trilinear(g8, fx, fy, fz, gx, gy, gz);
-            float h[3], hk[3];
-#pragma unroll
-            for (int c = 0; c < 3; c++) {
-                h[c] = wrun * (dr[c] * Q + rho * dQ[c]);
-                hk[c] = al * h[c];
-            }
-            add_pose(h, hk, owner);
-        }
-    };
+    auto add_pose = [&](const float h[3], const float hk[3], int owner) { add_pose_sums<M>(sh, lane, h, hk, owner); };
 
     // Drains `count` (<= 32) queued runs starting at ring slot `first`, one run per lane. Each run is
     // re-derived from its first alpha with the march's own float32 operations, so its positions,
@@ -332,6 +401,7 @@ __global__ void __launch_bounds__(kBlockThreads, 5) adjoint_kernel(const __grid_
         const int e = (first + lane) & (kAdjQueue - 1);
         float al = 0.0f, wrun = 1.0f;
         int kn = 0, owner = 0;
+        uint32_t word = 0;
         bool mixed = false;
         if (mine) {
             al = __uint_as_float(sh.run[0][e]);
@@ -343,7 +413,7 @@ __global__ void __launch_bounds__(kBlockThreads, 5) adjoint_kernel(const __grid_
             const float py = __fsub_rn(__fmaf_rn(al, ryi, sh.ray[4][owner]), 1.0f);
             const float pz = __fsub_rn(__fmaf_rn(al, rzi, sh.ray[5][owner]), 1.0f);
             const float bx = floorf(px), by = floorf(py), bz = floorf(pz);
-            const uint32_t word = fetch_label_word(V, bx, by, bz);
+            word = fetch_label_word(V, bx, by, bz);
             mixed = !uniform_word(word);
             float r8[8];
             if (do_pose && !mixed) {
@@ -413,37 +483,21 @@ __global__ void __launch_bounds__(kBlockThreads, 5) adjoint_kernel(const __grid_
                 }
             }
         }
-        // mixed-label runs: their samples, numbered across the warp, 32 at a time
-        int nmix = mixed ? kn : 0;
-        int off = nmix;  // inclusive prefix sum over the lanes
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int x = __shfl_up_sync(kAll, off, o);
-            if (lane >= o) off += x;
+        // runs in mixed-label cells wait in their own ring until 32 of them can go at once
+        const unsigned mm = __ballot_sync(kAll, mixed);
+        if (mixed) {
+            const int s = (mhead + mqueued + __popc(mm & lt)) & (kAdjQueue - 1);
+            sh.mix[0][s] = __float_as_uint(al);
+            sh.mix[1][s] = sh.run[1][e];
+            sh.mix[2][s] = word;
         }
-        const int total = __shfl_sync(kAll, off, 31);
-        for (int base = 0; base < total; base += 32) {
-            const int g = base + lane;
-            // the run holding sample g: the first lane whose inclusive prefix exceeds g
-            int src = 0;
-#pragma unroll
-            for (int b = 16; b > 0; b >>= 1) {
-                const int cand = src + b;
-                const int o_c = __shfl_sync(kAll, off, cand - 1);
-                if (o_c <= g) src = cand;
-            }
-            // every lane takes part in every shuffle (lane src - 1 wraps to 31 for src = 0)
-            const int o_before = __shfl_sync(kAll, off, (src + 31) & 31);
-            const int o_prev = src > 0 ? o_before : 0;
-            const float s_al = __shfl_sync(kAll, al, src);
-            const int s_owner = __shfl_sync(kAll, owner, src) & 31;
-            const float s_w = __shfl_sync(kAll, wrun, src);
-            if (g < total) {
-                float a = s_al;
-                // exactly g - o_prev (< 255) additions from the run's first alpha
-                advance_alpha(&a, step, __int_as_float(0x7f800000), min(max(g - o_prev, 0), 254), false);
-                mixed_sample(a, s_owner, s_w);
-            }
+        mqueued += __popc(mm);
+        if (mqueued >= 32) {
+            __syncwarp();
+            drain_mixed<M>(P, sh, lane, mhead, 32);
+            __syncwarp();
+            mhead = (mhead + 32) & (kAdjQueue - 1);
+            mqueued -= 32;
         }
     };
 
@@ -454,8 +508,6 @@ __global__ void __launch_bounds__(kBlockThreads, 5) adjoint_kernel(const __grid_
     const bool first_half = ray_live && R.t == 0;
     const bool last_half = ray_live && R.t_end == R.num_steps && R.num_steps > 1;
     const int t_stop = last_half ? R.num_steps - 1 : R.t_end;  // end of the full-weight samples
-    int head = 0, queued = 0;  // warp-uniform ring state
-    const unsigned lt = (1u << lane) - 1u;
 
     // the open run: sample count, first alpha, label cell, filter fixed point, packed sums
     int K = 0;
@@ -552,6 +604,8 @@ __global__ void __launch_bounds__(kBlockThreads, 5) adjoint_kernel(const __grid_
     single(last_half);
     __syncwarp();
     drain(head, queued);
+    __syncwarp();
+    drain_mixed<M>(P, sh, lane, mhead, mqueued);
 
     if (do_pose) {
         // the warp's pose sums: one atomic per component
