@@ -452,29 +452,29 @@ __global__ void __launch_bounds__(kBlockThreads, 5) adjoint_kernel(const __grid_
                     const float y3 = (r8[7] - r8[5]) - (r8[6] - r8[4]) - (r8[3] - r8[1]) + ey;
                     const float z1 = (r8[5] - r8[1]) - ez, z2 = (r8[6] - r8[2]) - ez;
                     const float z3 = (r8[7] - r8[3]) - (r8[6] - r8[2]) - (r8[5] - r8[1]) + ez;
+                    // about the run's middle sample k_c = (K - 1) / 2 the odd sums of k - k_c vanish:
+                    // sum g(f_k) and sum alpha_k g(f_k) need only S2 = sum (k - k_c)^2 = K (K^2 - 1) / 12
                     const float kf = (float)kn;
-                    const float T1 = 0.5f * kf * (kf - 1.0f);                   // sum k
-                    const float T2 = T1 * (2.0f * kf - 1.0f) * (1.0f / 3.0f);  // sum k^2
-                    const float T3 = T1 * T1;                                   // sum k^3
-                    // moment of g: m = sum g(f_k), n = sum alpha_k g(f_k) = alpha0 m + delta sum k g(f_k)
+                    const float kc = 0.5f * kf - 0.5f;
+                    const float cx = ax + kc * bxs, cy = ay + kc * bys, cz = az + kc * bzs;
+                    const float ac = al + kc * delta;
+                    const float S2 = kf * (kf * kf - 1.0f) * (1.0f / 12.0f);
+                    const float dS2 = delta * S2;
                     float h[3], hk[3];
-                    float m = kf, n = al * kf + delta * T1;  // g = 1
+                    float m = kf, n = ac * kf;  // g = 1
                     h[0] = ex * m, h[1] = ey * m, h[2] = ez * m;
                     hk[0] = ex * n, hk[1] = ey * n, hk[2] = ez * n;
-                    m = kf * ax + bxs * T1, n = al * m + delta * (ax * T1 + bxs * T2);  // g = f_x
+                    m = kf * cx, n = ac * m + dS2 * bxs;  // g = f_x
                     h[1] += y1 * m, h[2] += z1 * m, hk[1] += y1 * n, hk[2] += z1 * n;
-                    m = kf * ay + bys * T1, n = al * m + delta * (ay * T1 + bys * T2);  // g = f_y
+                    m = kf * cy, n = ac * m + dS2 * bys;  // g = f_y
                     h[0] += x1 * m, h[2] += z2 * m, hk[0] += x1 * n, hk[2] += z2 * n;
-                    m = kf * az + bzs * T1, n = al * m + delta * (az * T1 + bzs * T2);  // g = f_z
+                    m = kf * cz, n = ac * m + dS2 * bzs;  // g = f_z
                     h[0] += x2 * m, h[1] += y2 * m, hk[0] += x2 * n, hk[1] += y2 * n;
-                    float c0 = ax * ay, c1 = ax * bys + ay * bxs, c2 = bxs * bys;  // g = f_x f_y
-                    m = kf * c0 + c1 * T1 + c2 * T2, n = al * m + delta * (c0 * T1 + c1 * T2 + c2 * T3);
+                    m = kf * cx * cy + bxs * bys * S2, n = ac * m + dS2 * (cx * bys + cy * bxs);  // g = f_x f_y
                     h[2] += z3 * m, hk[2] += z3 * n;
-                    c0 = ax * az, c1 = ax * bzs + az * bxs, c2 = bxs * bzs;  // g = f_x f_z
-                    m = kf * c0 + c1 * T1 + c2 * T2, n = al * m + delta * (c0 * T1 + c1 * T2 + c2 * T3);
+                    m = kf * cx * cz + bxs * bzs * S2, n = ac * m + dS2 * (cx * bzs + cz * bxs);  // g = f_x f_z
                     h[1] += y3 * m, hk[1] += y3 * n;
-                    c0 = ay * az, c1 = ay * bzs + az * bys, c2 = bys * bzs;  // g = f_y f_z
-                    m = kf * c0 + c1 * T1 + c2 * T2, n = al * m + delta * (c0 * T1 + c1 * T2 + c2 * T3);
+                    m = kf * cy * cz + bys * bzs * S2, n = ac * m + dS2 * (cy * bzs + cz * bys);  // g = f_y f_z
                     h[0] += x3 * m, hk[0] += x3 * n;
                     const float gw = gu * wrun;
 #pragma unroll
