@@ -17,17 +17,18 @@
 //
 // One kernel computes both. Each thread marches one ray over exactly the forward's samples (same
 // float32 alpha sequence, same live step range, same trapezoid half weights); the 32 rays of a warp
-// step together. A ray's samples fall into runs: a density run is a stretch of samples in one
-// texture-filter cell with one value of w_t q_t, a pose run a stretch in one label cell with one
-// trapezoid weight. Within a run the per-sample work is small and identical across the warp: the
-// eight integer corner weights are summed two to a register (drr_texweights.h), and a pose run only
-// counts its samples. When a run ends, the ray appends it to a per-warp queue in shared memory; the
-// warp drains the queues together once they are half full, so the per-cell work -- eight texel
-// additions to the gradient volume per density run, eight texel fetches and the gradient sums per
-// pose run -- runs with all lanes busy instead of once per lane that happens to change cell.
-// A pose run in a cell whose eight labels agree is summed in closed form: Q is constant there and
-// grad rho is bilinear in the fractions, so its sums over the run's evenly spaced samples are
-// polynomials in the run length; runs in mixed cells are evaluated sample by sample in the drain.
+// step together. A ray's full-weight samples fall into runs: stretches with one label cell and one
+// texture-filter cell (the two half-weight samples are runs of their own). Within a run the
+// per-sample work is small and identical across the warp: the eight integer corner weights are
+// summed two to a register (drr_texweights.h). When a run ends, the ray appends its first alpha,
+// length and sums to a per-warp ring in shared memory; once 32 runs wait, the warp drains them,
+// one run per lane, so the per-cell work -- the label word, eight texel additions to the gradient
+// volume, eight texel fetches and the pose sums -- runs with all lanes busy instead of once per
+// lane that happens to change cell. The drain re-derives a run's positions from its first alpha
+// with the march's own float32 operations. A run in a cell whose eight labels agree is summed in
+// closed form: q and Q are constant there and grad rho is bilinear in the fractions, so the pose
+// sums over the run's evenly spaced samples are polynomials in the run length. Runs in cells with
+// mixed labels wait in a second ring and are then split into their samples, 32 evaluated at once.
 // Only single-volume projections without air attenuation outside the volume are differentiated.
 #pragma once
 
