@@ -493,9 +493,140 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
             ++t;
         }
         if (cur_m >= 0) store_ad<M>(ad, cur_m, cur_ad);
+    } else if (NV > 1 && !p.full_march && !carve) {
+        // Several volumes between the first interval's entry and the last one's exit: the
+        // reference's step (project_kernel.cu:394-553) with the same results, cheaper per step.
+        //   * The set of volumes whose interval holds alpha changes only where alpha passes an
+        //     interval end, so the priority resolution (project_kernel.cu:458-496), the 1/n weight
+        //     and the mask of adding volumes are redone only there (`enter`: the next interval
+        //     start ahead, `leave`: the nearest end of a live interval).
+        //   * The label cache (project_kernel.cu:394-431) is keyed by the last base any enabled
+        //     volume moved it to, so the key still follows every enabled volume each step. The word
+        //     it holds is a function of (the volume that set the key, the key): when an adding volume
+        //     set the key itself, that is its own word at its own base, which was loaded a step ahead;
+        //     when another volume's base coincides with it (the reference's cross-volume quirk), the
+        //     word is loaded from that volume's labels, as the reference's cache holds it.
+        //   * Uniform and two-label cells take the single-volume path's shortcuts (same additions).
+        int cur = NV, n = 0;
+        unsigned adds = 0;  // volumes adding at priority `cur` (no range re-check, project_kernel.cu:541)
+        float wseg = 0.0f;  // 1 / n
+        float enter = -__int_as_float(0x7f800000), leave = __int_as_float(0x7f800000);
+        auto resolve = [&]() {
+            cur = NV, n = 0;
+            enter = __int_as_float(0x7f800000), leave = __int_as_float(0x7f800000);
+#pragma unroll
+            for (int i = 0; i < NV; i++) {
+                if (!trace[i]) continue;
+                if (alpha < minv[i]) {
+                    enter = fminf(enter, minv[i]);
+                    continue;
+                }
+                if (alpha > maxv[i]) continue;
+                leave = fminf(leave, maxv[i]);
+                const int pr = p.vol[i].priority;
+                if (pr < cur) {
+                    cur = pr;
+                    n = 1;
+                } else if (pr == cur) {
+                    n += 1;
+                }
+            }
+            adds = 0u;
+            if (n != 0) {
+#pragma unroll
+                for (int i = 0; i < NV; i++)
+                    if (trace[i] && p.vol[i].priority == cur) adds |= 1u << i;
+            }
+            wseg = n != 0 ? __fdiv_rn(1.0f, (float)n) : 0.0f;
+        };
+        int key_vol = -1;  // volume whose labels the cached word comes from; the key is (pb0, pb1, pb2)
+        uint32_t w_pre[NV];
+        unsigned pre_ok = 0u;  // volumes whose word at this step's base was loaded a step ahead
+#pragma unroll
+        for (int i = 0; i < NV; i++) w_pre[i] = 0u;
+        int cur_m = -1;  // material whose accumulator is held in cur_ad
+        float cur_ad = 0.0f;
+        auto msample = [&](float half) {
+            if (alpha >= enter || alpha > leave) resolve();
+            const float weight = __fmul_rn(wseg, half);  // fl(1/n) * 0.5 is exact
+            if (n == 0 && attenuate) {
+                if (cur_m == air)
+                    cur_ad = add_air(cur_ad);
+                else
+                    store_ad<M>(ad, air, add_air(load_ad<M>(ad, air)));
+            }
+            const float an = __fadd_rn(alpha, step);
+            unsigned pre_next = 0u;
+#pragma unroll
+            for (int vol = 0; vol < NV; vol++) {
+                if (!p.vol[vol].enabled) continue;
+                const float *s = view.vol[vol].s;
+                const float px = __fsub_rn(__fmaf_rn(alpha, rxi[vol], s[0]), 1.0f);
+                const float py = __fsub_rn(__fmaf_rn(alpha, ryi[vol], s[1]), 1.0f);
+                const float pz = __fsub_rn(__fmaf_rn(alpha, rzi[vol], s[2]), 1.0f);
+                const float bx = floorf(px), by = floorf(py), bz = floorf(pz);
+                if (bx != pb0 || by != pb1 || bz != pb2) {
+                    pb0 = bx, pb1 = by, pb2 = bz;
+                    key_vol = vol;
+                }
+                if (!((adds >> vol) & 1u)) continue;
+                uint32_t w;
+                if (key_vol == vol) {
+                    w = (pre_ok >> vol) & 1u ? w_pre[vol] : fetch_label_word(p.vol[vol], bx, by, bz);
+                } else {
+                    w = 0u;
+#pragma unroll
+                    for (int i = 0; i < NV; i++)
+                        if (i == key_vol) w = fetch_label_word(p.vol[i], pb0, pb1, pb2);
+                }
+                {  // this volume's word at the next step's base, loaded now
+                    const float nx = __fsub_rn(__fmaf_rn(an, rxi[vol], s[0]), 1.0f);
+                    const float ny = __fsub_rn(__fmaf_rn(an, ryi[vol], s[1]), 1.0f);
+                    const float nz = __fsub_rn(__fmaf_rn(an, rzi[vol], s[2]), 1.0f);
+                    w_pre[vol] = fetch_label_word(p.vol[vol], floorf(nx), floorf(ny), floorf(nz));
+                    pre_next |= 1u << vol;
+                }
+                const CornerWeights cw = corner_weights(__fsub_rn(px, bx), __fsub_rn(py, by), __fsub_rn(pz, bz));
+                const float rho = tex3D<float>(p.vol[vol].density, __fadd_rn(px, 0.5f), __fadd_rn(py, 0.5f),
+                                               __fadd_rn(pz, 0.5f));
+                const float wr = __fmul_rn(weight, rho);
+                if (uniform_word(w)) {
+                    const int L = (int)(w & 15u);
+                    const float su = uniform_sum(cw);
+                    if (L != cur_m) {
+                        if (cur_m >= 0) store_ad<M>(ad, cur_m, cur_ad);
+                        cur_ad = load_ad<M>(ad, L);
+                        cur_m = L;
+                    }
+                    cur_ad = __fmaf_rn(wr, su, cur_ad);
+                } else {
+                    if (cur_m >= 0) store_ad<M>(ad, cur_m, cur_ad);
+                    cur_m = -1;
+                    float seg[M];
+                    label_fractions<M>(w, cw, seg);
+#pragma unroll
+                    for (int m = 0; m < M; m++) ad[m] = __fmaf_rn(wr, seg[m], ad[m]);
+                }
+            }
+            pre_ok = pre_next;
+            alpha = an;
+        };
+        if (t < t_end && t == 0) {
+            msample(0.5f);
+            ++t;
+        }
+        const bool last_half = t < t_end && t_end == num_steps;
+        const int t_main = last_half ? t_end - 1 : t_end;
+        for (; t < t_main; ++t) msample(1.0f);
+        if (last_half) {
+            msample(0.5f);
+            ++t;
+        }
+        if (cur_m >= 0) store_ad<M>(ad, cur_m, cur_ad);
     } else {
-        // Several volumes (or DRR_FLAG_FULL_MARCH): the reference's step. The label cache is keyed by
-        // the last base any enabled volume moved it to (project_kernel.cu:394-431), and a volume whose
+        // DRR_FLAG_FULL_MARCH or subtractive meshes, any number of volumes: the reference's step. The
+        // label cache is keyed by the last base any enabled volume moved it to
+        // (project_kernel.cu:394-431), and a volume whose
         // base equals the key reads the cached word even if another volume's texture filled it. The
         // key therefore follows every enabled volume each step, but the word is only fetched when a
         // contributing volume needs it, from the texture of the volume that set the key: the same

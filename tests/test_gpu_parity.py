@@ -168,6 +168,33 @@ def test_multi_volume_matches_oracle_and_full_march():
         assert np.all(d <= 2e-6 * np.abs(ref["area_density"]) + 1e-7), d.max()
 
 
+def test_coincident_volumes_share_the_label_cache():
+    """Two volumes on the same voxel grid (a CT and a second segmentation of it, plus a third volume
+    elsewhere): their bases coincide at every step, so the reference's label cache hands one volume
+    the other's cached labels (project_kernel.cu:394-431). The batched path must reproduce that:
+    bit-identical to the full march, and within float32 rounding of the oracle."""
+    rng = np.random.default_rng(21)
+    hu = simple_phantom_hu(36, seed=21)
+    a = volume_from_hu(hu)
+    names, seg = a.materials
+    relabel = {"soft tissue": seg == names["bone"], "bone": seg == names["soft tissue"], "air": seg == names["air"]}
+    b = dd.Volume.from_parameters(a.data * 0.5, relabel, origin=-(np.asarray(hu.shape) - 1) / 2.0, spacing=(1.0, 1.0, 1.0))
+    c = implant_volume((16, 16, 12), seed=22)
+    c.world_from_anatomical = random_rigid(rng, 5.0, 30.0)
+    projs = random_views(2, a.center_in_world, seed=23, sphere_mm=3.0, sensor_size=(20, 18), pixel_size=3.0)
+    for prio in (None, [0, 1, 2], [1, 1, 0]):
+        vols = [a, b, c]
+        got = run_product(vols, projs, priorities=prio)
+        full = run_product(vols, projs, priorities=prio, flags=_lib.DRR_FLAG_FULL_MARCH)
+        for k in ("intensity", "area_density"):
+            np.testing.assert_array_equal(got[k], full[k])
+        for i, proj in enumerate(projs):
+            ref = oracle_scene(vols, proj, priorities=prio).project("f32")
+            assert rel_err(got["intensity"][i], ref["intensity"]).max() <= 2e-6
+            d = np.abs(got["area_density"][i] - ref["area_density"])
+            assert np.all(d <= 2e-6 * np.abs(ref["area_density"]) + 1e-7), d.max()
+
+
 def test_attenuate_outside_matches_oracle():
     vols, projs = small_scene(6)
     got = run_product(vols, projs, attenuate=True)
