@@ -505,7 +505,11 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
         //     it holds is a function of (the volume that set the key, the key): when an adding volume
         //     set the key itself, that is its own word at its own base, which was loaded a step ahead;
         //     when another volume's base coincides with it (the reference's cross-volume quirk), the
-        //     word is loaded from that volume's labels, as the reference's cache holds it.
+        //     word is loaded from that volume's labels, as the reference's cache holds it. Two
+        //     volumes' bases can only coincide where their IJK positions, affine in alpha, are within
+        //     a voxel (plus a step, for the previous step's key) on every axis: an interval of alpha
+        //     per pair, computed once per ray. Outside the hull of those intervals the key is always
+        //     the adding volume's own base, so the other volumes are not followed there at all.
         //   * Uniform and two-label cells take the single-volume path's shortcuts (same additions).
         int cur = NV, n = 0;
         unsigned adds = 0;  // volumes adding at priority `cur` (no range re-check, project_kernel.cu:541)
@@ -539,6 +543,40 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
             }
             wseg = n != 0 ? __fdiv_rn(1.0f, (float)n) : 0.0f;
         };
+        // alpha range where two enabled volumes' bases may coincide (0.05 voxel of slack for rounding)
+        float dlo = __int_as_float(0x7f800000), dhi = -__int_as_float(0x7f800000);
+        int last_vol = -1;  // the last enabled volume: it sets the key at the end of a step
+#pragma unroll
+        for (int u = 0; u < NV; u++) {
+            if (!p.vol[u].enabled) continue;
+            last_vol = u;
+#pragma unroll
+            for (int v = u + 1; v < NV; v++) {
+                if (!p.vol[v].enabled) continue;
+                const float ru[3] = {rxi[u], ryi[u], rzi[u]}, rv[3] = {rxi[v], ryi[v], rzi[v]};
+                double lo = -1e300, hi = 1e300;
+#pragma unroll
+                for (int ax = 0; ax < 3; ax++) {
+                    // |(s_v - s_u) + alpha (r_v - r_u)| < band on this axis
+                    const double a = (double)view.vol[v].s[ax] - (double)view.vol[u].s[ax];
+                    const double b = (double)rv[ax] - (double)ru[ax];
+                    const double band = 1.05 + (double)step * fmax(fabs((double)ru[ax]), fabs((double)rv[ax]));
+                    if (fabs(b) < 1e-12) {
+                        if (!(fabs(a) < band)) lo = 1e300, hi = -1e300;
+                    } else {
+                        const double x0 = (-band - a) / b, x1 = (band - a) / b;
+                        lo = fmax(lo, fmin(x0, x1));
+                        hi = fmin(hi, fmax(x0, x1));
+                    }
+                }
+                if (lo <= hi) {
+                    dlo = fminf(dlo, (float)(lo - (double)step));
+                    dhi = fmaxf(dhi, (float)(hi + (double)step));
+                }
+            }
+        }
+        bool tracking = false;  // the previous step followed the key through every enabled volume
+        float alpha_prev = __int_as_float(0x7fc00000);  // NaN before the first step: the key starts empty
         int key_vol = -1;  // volume whose labels the cached word comes from; the key is (pb0, pb1, pb2)
         uint32_t w_pre[NV];
         unsigned pre_ok = 0u;  // volumes whose word at this step's base was loaded a step ahead
@@ -556,22 +594,37 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
                     store_ad<M>(ad, air, add_air(load_ad<M>(ad, air)));
             }
             const float an = __fadd_rn(alpha, step);
+            const bool track = alpha >= dlo && alpha <= dhi;
+            if (track && !tracking) {
+                // entering the range: the key as the previous step left it, the last volume's base
+#pragma unroll
+                for (int i = 0; i < NV; i++) {
+                    if (i != last_vol) continue;
+                    const float *s = view.vol[i].s;
+                    pb0 = floorf(__fsub_rn(__fmaf_rn(alpha_prev, rxi[i], s[0]), 1.0f));
+                    pb1 = floorf(__fsub_rn(__fmaf_rn(alpha_prev, ryi[i], s[1]), 1.0f));
+                    pb2 = floorf(__fsub_rn(__fmaf_rn(alpha_prev, rzi[i], s[2]), 1.0f));
+                    key_vol = i;
+                }
+            }
+            tracking = track;
             unsigned pre_next = 0u;
 #pragma unroll
             for (int vol = 0; vol < NV; vol++) {
                 if (!p.vol[vol].enabled) continue;
+                if (!track && !((adds >> vol) & 1u)) continue;
                 const float *s = view.vol[vol].s;
                 const float px = __fsub_rn(__fmaf_rn(alpha, rxi[vol], s[0]), 1.0f);
                 const float py = __fsub_rn(__fmaf_rn(alpha, ryi[vol], s[1]), 1.0f);
                 const float pz = __fsub_rn(__fmaf_rn(alpha, rzi[vol], s[2]), 1.0f);
                 const float bx = floorf(px), by = floorf(py), bz = floorf(pz);
-                if (bx != pb0 || by != pb1 || bz != pb2) {
+                if (track && (bx != pb0 || by != pb1 || bz != pb2)) {
                     pb0 = bx, pb1 = by, pb2 = bz;
                     key_vol = vol;
                 }
                 if (!((adds >> vol) & 1u)) continue;
                 uint32_t w;
-                if (key_vol == vol) {
+                if (!track || key_vol == vol) {
                     w = (pre_ok >> vol) & 1u ? w_pre[vol] : fetch_label_word(p.vol[vol], bx, by, bz);
                 } else {
                     w = 0u;
@@ -609,6 +662,7 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
                 }
             }
             pre_ok = pre_next;
+            alpha_prev = alpha;
             alpha = an;
         };
         if (t < t_end && t == 0) {
