@@ -434,11 +434,13 @@ def main():
     comp = metrics.compulsory_bytes(vols, W, H, args.density_dtype)
     launch_s = ms_per_step / 1000.0 / nviews
     achieved = comp / launch_s / 1e9
-    traffic = None
+    traffic = tex_pipe = None
     if TRAFFIC_FILE.exists():
         for ln in TRAFFIC_FILE.read_text().splitlines():
             if ln.startswith("dram_bytes_per_launch:"):
                 traffic = float(ln.split(":")[1])
+            elif ln.startswith("tex_pipe_pct:"):
+                tex_pipe = float(ln.split(":")[1])
     sampled_bytes = samples_per_step / nviews * metrics.BYTES_PER_SAMPLE[args.density_dtype]
     line = {
         "metric": METRIC, "value": value, "unit": "projections/s", "n_gpus": world, "steps": args.steps,
@@ -462,7 +464,9 @@ def main():
                      "note": "compulsory bytes (each voxel's density+label once, plus output images) per view; "
                              "peak = measured copy bandwidth of MEASURED_PEAKS.json"},
         "sampled": {"bytes_per_launch": sampled_bytes, "gb_per_s": sampled_bytes / launch_s / 1e9,
-                    "note": "texel bytes the march reads per view (40 B/sample at float32), served by L1/TEX"},
+                    "tex_pipe_pct_of_peak_ncu": tex_pipe,
+                    "note": "texel bytes the march reads per view (40 B/sample at float32), served by L1/TEX; "
+                            "texture-pipe utilisation from the ncu capture in profiles/"},
         "e2e": e2e,
     }
     if rank == 0 and not args.no_cpu_baseline:
