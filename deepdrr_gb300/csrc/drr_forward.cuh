@@ -808,9 +808,20 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
     if (p.solid_angle != nullptr) p.solid_angle[vout * plane + pix] = pixel_solid_angle(view.w, u, v);
 }
 
+// Resident blocks per SM the forward kernels are compiled for: the march is issue- and latency-
+// bound, and more warps hide its load and texture latency. Measured on GB300: 8 blocks of 128
+// threads (64 registers) for one volume with 4 materials (+1 % over the compiler's 72 registers)
+// and for three volumes with 4 materials (+25 % over its 96, with 72 bytes of spills). The other
+// buckets take the most blocks that keep spills under ~80 bytes; 16 materials keep the
+// compiler's choice.
+template <int NV, int M>
+constexpr int forward_min_blocks() {
+    return M > 8 ? 1 : (NV <= 2 ? 8 : (NV == 3 ? (M <= 4 ? 8 : 7) : (M <= 4 ? 7 : 6)));
+}
+
 // Plain launch: one block per 16 x 8 pixel tile (each warp an 8 x 4 pixel sub-tile), z = view.
 template <int NV, int M>
-__global__ void __launch_bounds__(kBlockThreads) forward_kernel(const __grid_constant__ ForwardParams<NV> p) {
+__global__ void __launch_bounds__(kBlockThreads, forward_min_blocks<NV, M>()) forward_kernel(const __grid_constant__ ForwardParams<NV> p) {
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const int u = blockIdx.x * kTileW + ((warp & 1) << 3) + (lane & 7);
@@ -825,7 +836,7 @@ __global__ void __launch_bounds__(kBlockThreads) forward_kernel(const __grid_con
 // in L2. Rays of uneven length therefore balance across the GPU. Every block ends once the counter
 // passes the last item; the loop has no waits.
 template <int NV, int M>
-__global__ void __launch_bounds__(kBlockThreads) forward_persistent_kernel(const __grid_constant__ PersistentParams<NV> p) {
+__global__ void __launch_bounds__(kBlockThreads, forward_min_blocks<NV, M>()) forward_persistent_kernel(const __grid_constant__ PersistentParams<NV> p) {
     __shared__ unsigned int s_first;
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
