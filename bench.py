@@ -434,13 +434,18 @@ def main():
     comp = metrics.compulsory_bytes(vols, W, H, args.density_dtype)
     launch_s = ms_per_step / 1000.0 / nviews
     achieved = comp / launch_s / 1e9
-    traffic = tex_pipe = None
+    traffic = tex_pipe = l1_hit = l2_hit = None
     if TRAFFIC_FILE.exists():
         for ln in TRAFFIC_FILE.read_text().splitlines():
-            if ln.startswith("dram_bytes_per_launch:"):
-                traffic = float(ln.split(":")[1])
-            elif ln.startswith("tex_pipe_pct:"):
-                tex_pipe = float(ln.split(":")[1])
+            key, _, val = ln.partition(":")
+            if key == "dram_bytes_per_launch":
+                traffic = float(val)
+            elif key == "tex_pipe_pct":
+                tex_pipe = float(val)
+            elif key == "l1tex_hit_pct":
+                l1_hit = float(val)
+            elif key == "l2_hit_pct":
+                l2_hit = float(val)
     sampled_bytes = samples_per_step / nviews * metrics.BYTES_PER_SAMPLE[args.density_dtype]
     line = {
         "metric": METRIC, "value": value, "unit": "projections/s", "n_gpus": world, "steps": args.steps,
@@ -464,7 +469,7 @@ def main():
                      "note": "compulsory bytes (each voxel's density+label once, plus output images) per view; "
                              "peak = measured copy bandwidth of MEASURED_PEAKS.json"},
         "sampled": {"bytes_per_launch": sampled_bytes, "gb_per_s": sampled_bytes / launch_s / 1e9,
-                    "tex_pipe_pct_of_peak_ncu": tex_pipe,
+                    "tex_pipe_pct_of_peak_ncu": tex_pipe, "l1tex_hit_pct_ncu": l1_hit, "l2_hit_pct_ncu": l2_hit,
                     "note": "texel bytes the march reads per view (40 B/sample at float32), served by L1/TEX; "
                             "texture-pipe utilisation from the ncu capture in profiles/"},
         "e2e": e2e,
