@@ -347,10 +347,12 @@ __device__ __forceinline__ void drain_mixed(const AdjointParams &P, AdjointWarpS
 // Density and pose gradients of one view per blockIdx.z, one ray per thread (16 x 8 pixel tiles,
 // each warp 8 x 4 pixels). A run is a stretch of a ray's full-weight samples with one label cell
 // and one texture-filter cell; the trapezoid half-weight samples (t = 0 and t = num_steps - 1) are
-// runs of their own. See the file comment. 5 blocks per SM (96 registers) balances occupancy
-// against the registers the drain needs.
+// runs of their own. See the file comment. Resident blocks per SM balance occupancy against the
+// registers the drain needs: measured with 3 materials, 6 blocks (80 registers, a few spills)
+// against 5 (96): 1.59 against 1.60 ms/view forward + backward; 7 and 8 blocks spill more and
+// are slower. More materials keep 5.
 template <int M>
-__global__ void __launch_bounds__(kBlockThreads, 5) adjoint_kernel(const __grid_constant__ AdjointParams P) {
+__global__ void __launch_bounds__(kBlockThreads, M <= 4 ? 6 : 5) adjoint_kernel(const __grid_constant__ AdjointParams P) {
     __shared__ AdjointWarpSmem<M> smem[kBlockThreads / 32];
     const SceneParams<1> &p = P.s;
     const int lane = threadIdx.x & 31;
@@ -416,13 +418,6 @@ __global__ void __launch_bounds__(kBlockThreads, 5) adjoint_kernel(const __grid_
             const float bx = floorf(px), by = floorf(py), bz = floorf(pz);
             word = fetch_label_word(V, bx, by, bz);
             mixed = !uniform_word(word);
-            float r8[8];
-            if (do_pose && !mixed) {
-#pragma unroll
-                for (int c = 0; c < 8; c++)
-                    r8[c] = tex3D<float>(P.density_point, bx + (float)(c & 1) + 0.5f,
-                                         by + (float)((c >> 1) & 1) + 0.5f, bz + (float)(c >> 2) + 0.5f);
-            }
             if (!mixed) {
                 const float gu = sh.gr[word & 15u][owner];
                 if (do_dens) {
@@ -441,6 +436,11 @@ __global__ void __launch_bounds__(kBlockThreads, 5) adjoint_kernel(const __grid_
                                  vals);
                 }
                 if (do_pose) {
+                    float r8[8];
+#pragma unroll
+                    for (int c = 0; c < 8; c++)
+                        r8[c] = tex3D<float>(P.density_point, bx + (float)(c & 1) + 0.5f,
+                                             by + (float)((c >> 1) & 1) + 0.5f, bz + (float)(c >> 2) + 0.5f);
                     // grad rho = c0 + c1 f_a + c2 f_b + c3 f_a f_b per axis (f_a, f_b the other two
                     // fractions), summed over the run's samples f0 + k d, alpha0 + k delta in closed form
                     const float ax = __fsub_rn(px, bx), ay = __fsub_rn(py, by), az = __fsub_rn(pz, bz);
