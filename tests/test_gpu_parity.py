@@ -168,11 +168,12 @@ def test_multi_volume_matches_oracle_and_full_march():
         assert np.all(d <= 2e-6 * np.abs(ref["area_density"]) + 1e-7), d.max()
 
 
-def test_coincident_volumes_share_the_label_cache():
-    """Two volumes on the same voxel grid (a CT and a second segmentation of it, plus a third volume
-    elsewhere): their bases coincide at every step, so the reference's label cache hands one volume
-    the other's cached labels (project_kernel.cu:394-431). The batched path must reproduce that:
-    bit-identical to the full march, and within float32 rounding of the oracle."""
+@pytest.mark.parametrize("nvol", [3, 4])
+def test_coincident_volumes_share_the_label_cache(nvol):
+    """Two volumes on the same voxel grid (a CT and a second segmentation of it, plus one or two
+    volumes elsewhere): their bases coincide at every step, so the reference's label cache hands one
+    volume the other's cached labels (project_kernel.cu:394-431). The batched path must reproduce
+    that: bit-identical to the full march, and within float32 rounding of the oracle."""
     rng = np.random.default_rng(21)
     hu = simple_phantom_hu(36, seed=21)
     a = volume_from_hu(hu)
@@ -181,9 +182,12 @@ def test_coincident_volumes_share_the_label_cache():
     b = dd.Volume.from_parameters(a.data * 0.5, relabel, origin=-(np.asarray(hu.shape) - 1) / 2.0, spacing=(1.0, 1.0, 1.0))
     c = implant_volume((16, 16, 12), seed=22)
     c.world_from_anatomical = random_rigid(rng, 5.0, 30.0)
+    fourth = volume_from_hu(simple_phantom_hu(20, seed=24), spacing=(1.3, 1.3, 1.3))
+    fourth.world_from_anatomical = random_rigid(rng, 6.0, 25.0)
     projs = random_views(2, a.center_in_world, seed=23, sphere_mm=3.0, sensor_size=(20, 18), pixel_size=3.0)
-    for prio in (None, [0, 1, 2], [1, 1, 0]):
-        vols = [a, b, c]
+    prios = (None, [0, 1, 2], [1, 1, 0]) if nvol == 3 else (None, [0, 1, 2, 3], [2, 2, 0, 1])
+    for prio in prios:
+        vols = [a, b, c, fourth][:nvol]
         got = run_product(vols, projs, priorities=prio)
         full = run_product(vols, projs, priorities=prio, flags=_lib.DRR_FLAG_FULL_MARCH)
         for k in ("intensity", "area_density"):
@@ -254,6 +258,27 @@ def test_multi_volume_matches_reference_kernel():
     mats = material_list(vols)
     _need_ref(2, len(mats))
     projs = random_views(2, a.center_in_world, seed=13, sphere_mm=3.0, sensor_size=(20, 18), pixel_size=3.0)
+    got = run_product(vols, projs)
+    for i, proj in enumerate(projs):
+        ref = ref_kernel.project(oracle_scene(vols, proj))
+        assert rel_err(got["intensity"][i], ref["intensity"]).max() <= 1e-4
+
+
+def test_coincident_volumes_match_reference_kernel():
+    """Three volumes, two of them on one voxel grid with different labels: the reference kernel's own
+    shared label cache decides which labels each of them reads."""
+    rng = np.random.default_rng(31)
+    hu = simple_phantom_hu(32, seed=31)
+    a = volume_from_hu(hu)
+    names, seg = a.materials
+    relabel = {"soft tissue": seg == names["bone"], "bone": seg == names["soft tissue"], "air": seg == names["air"]}
+    b = dd.Volume.from_parameters(a.data * 0.7, relabel, origin=-(np.asarray(hu.shape) - 1) / 2.0, spacing=(1.0, 1.0, 1.0))
+    c = implant_volume((16, 16, 12), seed=32)
+    c.world_from_anatomical = random_rigid(rng, 5.0, 30.0)
+    vols = [a, b, c]
+    mats = material_list(vols)
+    _need_ref(3, len(mats))
+    projs = random_views(2, a.center_in_world, seed=33, sphere_mm=3.0, sensor_size=(20, 18), pixel_size=3.0)
     got = run_product(vols, projs)
     for i, proj in enumerate(projs):
         ref = ref_kernel.project(oracle_scene(vols, proj))
