@@ -241,11 +241,12 @@ typedef struct {
     double center[3];               /* rotation centre, world */
 } drr_adjoint_args;
 
-/* Gradients of a loss through drr_project for one enabled volume without DRR_FLAG_ATTENUATE_OUTSIDE
- * (else DRR_ERR_UNSUPPORTED). The density gradient is the exact adjoint of the kernel's samples,
- * with the texture unit's 8-bit corner weights; the pose gradient differentiates the continuous
- * trilinear interpolation of the same texels and labels, with the march's sample positions held
- * fixed. No counterpart in the reference (its projector is not differentiable). */
+/* Gradients of a loss through drr_project for one enabled volume without DRR_FLAG_ATTENUATE_OUTSIDE,
+ * at most 32767 voxels per axis (else DRR_ERR_UNSUPPORTED). The density gradient is the exact
+ * adjoint of the kernel's samples, with the texture unit's 8-bit corner weights; the pose gradient
+ * differentiates the continuous trilinear interpolation of the same texels and labels, with the
+ * march's sample positions held fixed. No counterpart in the reference (its projector is not
+ * differentiable). */
 drr_status drr_project_adjoint(drr_volset *set, const drr_tables *tables, const drr_project_args *args,
                                const drr_adjoint_args *adjoint, void *stream);
 
