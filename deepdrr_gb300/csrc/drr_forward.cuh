@@ -671,7 +671,82 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
         }
         const bool last_half = t < t_end && t_end == num_steps;
         const int t_main = last_half ? t_end - 1 : t_end;
-        for (; t < t_main; ++t) msample(1.0f);
+        // A stretch where one volume adds and no two bases can coincide is a single-volume march:
+        // run it without the per-step interval and coincidence tests, its length counted in
+        // advance with the exact float32 fast-forward (drr_alpha.h).
+        auto single_stretch = [&]() -> bool {
+            if (alpha >= enter || alpha > leave) resolve();
+            if (n != 1 || __popc(adds) != 1 || (alpha >= dlo && alpha <= dhi)) return false;
+            const float bound = alpha < dlo ? fminf(enter, dlo) : enter;
+            float a = alpha;
+            int kk = advance_alpha(&a, step, bound, t_main - t, false);  // samples below the next start
+            a = alpha;
+            kk = min(kk, advance_alpha(&a, step, leave, kk, true));       // and not past the end
+            if (kk < 2) return false;
+            const int v = __ffs(adds) - 1;
+            float vrx = rxi[0], vry = ryi[0], vrz = rzi[0];
+            float vsx = view.vol[0].s[0], vsy = view.vol[0].s[1], vsz = view.vol[0].s[2];
+#pragma unroll
+            for (int i = 1; i < NV; i++)
+                if (i == v) {
+                    vrx = rxi[i], vry = ryi[i], vrz = rzi[i];
+                    vsx = view.vol[i].s[0], vsy = view.vol[i].s[1], vsz = view.vol[i].s[2];
+                }
+            const VolConst &Vv = p.vol[v];
+            const float weight = wseg;  // n = 1, full-weight samples
+            float cx = __fsub_rn(__fmaf_rn(alpha, vrx, vsx), 1.0f);
+            float cy = __fsub_rn(__fmaf_rn(alpha, vry, vsy), 1.0f);
+            float cz = __fsub_rn(__fmaf_rn(alpha, vrz, vsz), 1.0f);
+            float cbx = floorf(cx), cby = floorf(cy), cbz = floorf(cz);
+            uint32_t w_cur = 0u;
+#pragma unroll
+            for (int i = 0; i < NV; i++)
+                if (i == v) w_cur = (pre_ok >> i) & 1u ? w_pre[i] : fetch_label_word(Vv, cbx, cby, cbz);
+            for (int k = 0; k < kk; k++) {
+                const float an = __fadd_rn(alpha, step);
+                const float nx = __fsub_rn(__fmaf_rn(an, vrx, vsx), 1.0f);
+                const float ny = __fsub_rn(__fmaf_rn(an, vry, vsy), 1.0f);
+                const float nz = __fsub_rn(__fmaf_rn(an, vrz, vsz), 1.0f);
+                const float nbx = floorf(nx), nby = floorf(ny), nbz = floorf(nz);
+                const uint32_t w_next = fetch_label_word(Vv, nbx, nby, nbz);
+                const CornerWeights cw = corner_weights(__fsub_rn(cx, cbx), __fsub_rn(cy, cby), __fsub_rn(cz, cbz));
+                const float rho = tex3D<float>(Vv.density, __fadd_rn(cx, 0.5f), __fadd_rn(cy, 0.5f), __fadd_rn(cz, 0.5f));
+                const float wr = __fmul_rn(weight, rho);
+                if (uniform_word(w_cur)) {
+                    const int L = (int)(w_cur & 15u);
+                    const float su = uniform_sum(cw);
+                    if (L != cur_m) {
+                        if (cur_m >= 0) store_ad<M>(ad, cur_m, cur_ad);
+                        cur_ad = load_ad<M>(ad, L);
+                        cur_m = L;
+                    }
+                    cur_ad = __fmaf_rn(wr, su, cur_ad);
+                } else {
+                    if (cur_m >= 0) store_ad<M>(ad, cur_m, cur_ad);
+                    cur_m = -1;
+                    float seg[M];
+                    label_fractions<M>(w_cur, cw, seg);
+#pragma unroll
+                    for (int m = 0; m < M; m++) ad[m] = __fmaf_rn(wr, seg[m], ad[m]);
+                }
+                alpha_prev = alpha;
+                alpha = an;
+                cx = nx, cy = ny, cz = nz, cbx = nbx, cby = nby, cbz = nbz;
+                w_cur = w_next;
+            }
+#pragma unroll
+            for (int i = 0; i < NV; i++)
+                if (i == v) w_pre[i] = w_cur;
+            pre_ok = 1u << v;
+            tracking = false;
+            t += kk;
+            return true;
+        };
+        while (t < t_main) {
+            if (single_stretch()) continue;
+            msample(1.0f);
+            ++t;
+        }
         if (last_half) {
             msample(0.5f);
             ++t;
