@@ -42,6 +42,7 @@
 #include <stdint.h>
 
 #include "drr_alpha.h"
+#include "drr_coincide.h"
 
 namespace drr {
 
@@ -543,37 +544,23 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
             }
             wseg = n != 0 ? __fdiv_rn(1.0f, (float)n) : 0.0f;
         };
-        // alpha range where two enabled volumes' bases may coincide (0.05 voxel of slack for rounding)
-        float dlo = __int_as_float(0x7f800000), dhi = -__int_as_float(0x7f800000);
+        // alpha range where two enabled volumes' bases may coincide (drr_coincide.h), rounded outwards
+        float dlo, dhi;
         int last_vol = -1;  // the last enabled volume: it sets the key at the end of a step
+        {
+            bool en[NV];
+            float sv[NV][3], rv[NV][3];
 #pragma unroll
-        for (int u = 0; u < NV; u++) {
-            if (!p.vol[u].enabled) continue;
-            last_vol = u;
-#pragma unroll
-            for (int v = u + 1; v < NV; v++) {
-                if (!p.vol[v].enabled) continue;
-                const float ru[3] = {rxi[u], ryi[u], rzi[u]}, rv[3] = {rxi[v], ryi[v], rzi[v]};
-                double lo = -1e300, hi = 1e300;
-#pragma unroll
-                for (int ax = 0; ax < 3; ax++) {
-                    // |(s_v - s_u) + alpha (r_v - r_u)| < band on this axis
-                    const double a = (double)view.vol[v].s[ax] - (double)view.vol[u].s[ax];
-                    const double b = (double)rv[ax] - (double)ru[ax];
-                    const double band = 1.05 + (double)step * fmax(fabs((double)ru[ax]), fabs((double)rv[ax]));
-                    if (fabs(b) < 1e-12) {
-                        if (!(fabs(a) < band)) lo = 1e300, hi = -1e300;
-                    } else {
-                        const double x0 = (-band - a) / b, x1 = (band - a) / b;
-                        lo = fmax(lo, fmin(x0, x1));
-                        hi = fmin(hi, fmax(x0, x1));
-                    }
-                }
-                if (lo <= hi) {
-                    dlo = fminf(dlo, (float)(lo - (double)step));
-                    dhi = fmaxf(dhi, (float)(hi + (double)step));
-                }
+            for (int i = 0; i < NV; i++) {
+                en[i] = p.vol[i].enabled != 0;
+                if (en[i]) last_vol = i;
+                sv[i][0] = view.vol[i].s[0], sv[i][1] = view.vol[i].s[1], sv[i][2] = view.vol[i].s[2];
+                rv[i][0] = rxi[i], rv[i][1] = ryi[i], rv[i][2] = rzi[i];
             }
+            double lo, hi;
+            coincidence_range(NV, en, sv, rv, step, &lo, &hi);
+            dlo = lo <= hi ? __double2float_rd(lo) : __int_as_float(0x7f800000);
+            dhi = lo <= hi ? __double2float_ru(hi) : -__int_as_float(0x7f800000);
         }
         bool tracking = false;  // the previous step followed the key through every enabled volume
         float alpha_prev = __int_as_float(0x7fc00000);  // NaN before the first step: the key starts empty
