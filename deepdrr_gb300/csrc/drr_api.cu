@@ -97,6 +97,7 @@ void free_volume(Volume &v) {
     if (v.density_point) cudaDestroyTextureObject(v.density_point);
     if (v.density_array) cudaFreeArray(v.density_array);
     if (v.packed) cudaFree(v.packed);
+    if (v.coded) cudaFree(v.coded);
     v = Volume();
 }
 
@@ -104,9 +105,10 @@ void free_volume(Volume &v) {
 drr_status make_label_tables(const uint8_t *src, int ni, int nj, int nk, cudaStream_t s, Volume &v) {
     const size_t np = (size_t)(ni + 1) * (nj + 1) * (nk + 1);
     DRR_CUDA_TRY(cudaMalloc(&v.packed, np * sizeof(uint32_t)), "cudaMalloc (packed labels)");
+    DRR_CUDA_TRY(cudaMalloc(&v.coded, np * sizeof(uint32_t)), "cudaMalloc (coded labels)");
     const size_t blocks = (np + 255) / 256;
     drr::pack_labels_kernel<<<(unsigned)(blocks < 1048576 ? blocks : 1048576), 256, 0, s>>>(src, ni, nj, nk,
-                                                                                           v.packed);
+                                                                                           v.packed, v.coded);
     DRR_CUDA_TRY(cudaGetLastError(), "pack_labels_kernel launch");
     return DRR_OK;
 }
@@ -114,7 +116,8 @@ drr_status make_label_tables(const uint8_t *src, int ni, int nj, int nk, cudaStr
 }  // namespace
 
 namespace drr {
-__global__ void pack_labels_kernel(const uint8_t *__restrict__ labels, int ni, int nj, int nk, uint32_t *packed) {
+__global__ void pack_labels_kernel(const uint8_t *__restrict__ labels, int ni, int nj, int nk, uint32_t *packed,
+                                   uint32_t *coded) {
     const size_t np = (size_t)(ni + 1) * (nj + 1) * (nk + 1);
     for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < np; e += (size_t)gridDim.x * blockDim.x) {
         const int bi = (int)(e % (ni + 1)) - 1;
@@ -129,6 +132,22 @@ __global__ void pack_labels_kernel(const uint8_t *__restrict__ labels, int ni, i
             word |= ((uint32_t)labels[((size_t)k * nj + j) * ni + i] & 15u) << (4 * c);
         }
         packed[e] = word;
+        // A = corner 0's label, B = the first other label (A when there is none), the mask of the
+        // corners labelled B; bit 31 marks a neighbourhood with three or more labels
+        const uint32_t A = word & 15u;
+        uint32_t B = A, mask = 0u;
+        bool general = false;
+#pragma unroll
+        for (int c = 1; c < 8; c++) {
+            const uint32_t L = (word >> (4 * c)) & 15u;
+            if (L == A) continue;
+            if (B == A) B = L;
+            if (L == B)
+                mask |= 1u << c;
+            else
+                general = true;
+        }
+        coded[e] = general ? kCodeGeneral : (A | (B << 4) | (mask << 8));
     }
 }
 }  // namespace drr

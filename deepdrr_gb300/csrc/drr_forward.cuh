@@ -58,6 +58,7 @@ constexpr int kMaxSteps = 1 << 26;      // longest march per ray; longer rays ar
 struct VolConst {
     cudaTextureObject_t density;  // linear filter, clamp, unnormalised coordinates
     const uint32_t *packed;       // [(nk+1)][(nj+1)][(ni+1)] label words, see pack_labels_kernel
+    const uint32_t *coded;        // the same neighbourhoods as A | B << 4 | (corners labelled B) << 8
     int32_t n[3];                 // ni, nj, nk
     float hi[3];                  // n - 0.5 per axis (projector.py:1626-1634)
     float nm1[3];                 // n - 1 per axis
@@ -185,6 +186,17 @@ __device__ __forceinline__ uint32_t fetch_label_word(const VolConst &V, float bx
     const int j = (int)fminf(fmaxf(by, -1.0f), V.nm1[1]) + 1;
     const int k = (int)fminf(fmaxf(bz, -1.0f), V.nm1[2]) + 1;
     return __ldg(V.packed + ((size_t)k * (V.n[1] + 1) + j) * (V.n[0] + 1) + i);
+}
+
+// The same neighbourhood as a code: A (corner 0's label) | B << 4 (the other label, or A) |
+// (mask of the corners labelled B) << 8, or kCodeGeneral for three or more labels (then the word
+// itself is read). Built with the words by pack_labels_kernel.
+constexpr uint32_t kCodeGeneral = 0x80000000u;
+__device__ __forceinline__ uint32_t fetch_label_code(const VolConst &V, float bx, float by, float bz) {
+    const int i = (int)fminf(fmaxf(bx, -1.0f), V.nm1[0]) + 1;
+    const int j = (int)fminf(fmaxf(by, -1.0f), V.nm1[1]) + 1;
+    const int k = (int)fminf(fmaxf(bz, -1.0f), V.nm1[2]) + 1;
+    return __ldg(V.coded + ((size_t)k * (V.n[1] + 1) + j) * (V.n[0] + 1) + i);
 }
 
 __device__ __forceinline__ bool uniform_word(uint32_t w) { return w == (w & 15u) * 0x11111111u; }
@@ -420,7 +432,7 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
             cbx = floorf(cx);
             cby = floorf(cy);
             cbz = floorf(cz);
-            w_cur = fetch_label_word(V, cbx, cby, cbz);
+            w_cur = fetch_label_code(V, cbx, cby, cbz);
         }
         auto sample = [&](float wscale) {
             const float an = __fadd_rn(alpha, step);
@@ -428,11 +440,11 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
             const float ny = __fsub_rn(__fmaf_rn(an, ry0, sy), 1.0f);
             const float nz = __fsub_rn(__fmaf_rn(an, rz0, sz), 1.0f);
             const float nbx = floorf(nx), nby = floorf(ny), nbz = floorf(nz);
-            const uint32_t w_next = fetch_label_word(V, nbx, nby, nbz);
+            const uint32_t w_next = fetch_label_code(V, nbx, nby, nbz);
             const float px = cx, py = cy, pz = cz;
             const float fx = __fsub_rn(px, cbx), fy = __fsub_rn(py, cby), fz = __fsub_rn(pz, cbz);
-            word = w_cur;
-            const int uni_label = uniform_word(word) ? (int)(word & 15u) : -1;
+            const uint32_t code = w_cur;
+            const int uni_label = (code & (kCodeGeneral | 0xFF00u)) == 0u ? (int)(code & 15u) : -1;
             const CornerWeights cw = corner_weights(fx, fy, fz);
             const float rho = tex3D<float>(V.density, __fadd_rn(px, 0.5f), __fadd_rn(py, 0.5f), __fadd_rn(pz, 0.5f));
             const float wr = __fmul_rn(wscale, rho);
@@ -450,26 +462,21 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
                 // two labels A (corner 0's) and B: one pass over the corners into two sums, each
                 // in corner order as the reference accumulates them; other materials get
                 // fma(wr, 0, ad) = ad, exactly what the general path does for them
-                const uint32_t A = word & 15u;
-                const uint32_t xa = word ^ (A * 0x11111111u);
-                const int pos = (__ffs(xa) - 1) & ~3;
-                const uint32_t B = (word >> pos) & 15u;
-                const uint32_t xb = word ^ (B * 0x11111111u);
-                const uint32_t za = ~(((xa & 0x77777777u) + 0x77777777u) | xa) & 0x88888888u;
-                const uint32_t zb = ~(((xb & 0x77777777u) + 0x77777777u) | xb) & 0x88888888u;
-                if ((za | zb) == 0x88888888u) {
+                if (!(code & kCodeGeneral)) {
+                    const uint32_t A = code & 15u, B = (code >> 4) & 15u, mask = code >> 8;
                     float sA = 0.0f, sB = 0.0f;
 #pragma unroll
                     for (int c = 0; c < 8; c++) {
-                        if ((za >> (4 * c + 3)) & 1u)
-                            sA = __fmaf_rn(cw.xy[c & 3], cw.z[c >> 2], sA);
-                        else
+                        if ((mask >> c) & 1u)
                             sB = __fmaf_rn(cw.xy[c & 3], cw.z[c >> 2], sB);
+                        else
+                            sA = __fmaf_rn(cw.xy[c & 3], cw.z[c >> 2], sA);
                     }
 #pragma unroll
                     for (int m = 0; m < M; m++)
                         ad[m] = __fmaf_rn(wr, (uint32_t)m == A ? sA : ((uint32_t)m == B ? sB : 0.0f), ad[m]);
                 } else {
+                    word = fetch_label_word(V, cbx, cby, cbz);  // three or more labels: the corners' own
                     float seg[M];
                     label_fractions<M>(word, cw, seg);
 #pragma unroll
@@ -927,7 +934,8 @@ __global__ void __launch_bounds__(kBlockThreads, forward_min_blocks<NV, M>()) fo
 
 // Packs the labels of every 2x2x2 neighbourhood: word(b) for base b in [-1, n-1]^3 holds the labels
 // at clamp(b + d, 0, n - 1), corner c = dx | dy << 1 | dz << 2 in bits 4c..4c+3.
-__global__ void pack_labels_kernel(const uint8_t *__restrict__ labels, int ni, int nj, int nk, uint32_t *packed);
+__global__ void pack_labels_kernel(const uint8_t *__restrict__ labels, int ni, int nj, int nk, uint32_t *packed,
+                                   uint32_t *coded);
 
 // Host-side launcher, explicitly instantiated per (NV, M) in drr_inst_nv*.cu.
 template <int NV, int M>

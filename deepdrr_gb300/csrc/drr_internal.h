@@ -18,6 +18,7 @@ struct Volume {
     cudaTextureObject_t density_tex = 0;
     cudaTextureObject_t density_point = 0;  // point-filtered view of density_array (made by the adjoint)
     uint32_t *packed = nullptr;  // [(nk+1)][(nj+1)][(ni+1)] 2x2x2 label words
+    uint32_t *coded = nullptr;   // the same neighbourhoods as (A, B, corners labelled B), see pack_labels_kernel
     int ni = 0, nj = 0, nk = 0;
     int density_type = DRR_DENSITY_F32;
 };

@@ -65,6 +65,7 @@ void fill_scene(drr::SceneParams<NV> &p, const drr_volset *set, const drr_tables
         const drr::Volume &v = set->vol[i];
         p.vol[i].density = v.density_tex;
         p.vol[i].packed = v.packed;
+        p.vol[i].coded = v.coded;
         p.vol[i].n[0] = v.ni;
         p.vol[i].n[1] = v.nj;
         p.vol[i].n[2] = v.nk;
