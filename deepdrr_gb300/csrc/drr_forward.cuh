@@ -692,22 +692,20 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
             float cy = __fsub_rn(__fmaf_rn(alpha, vry, vsy), 1.0f);
             float cz = __fsub_rn(__fmaf_rn(alpha, vrz, vsz), 1.0f);
             float cbx = floorf(cx), cby = floorf(cy), cbz = floorf(cz);
-            uint32_t w_cur = 0u;
-#pragma unroll
-            for (int i = 0; i < NV; i++)
-                if (i == v) w_cur = (pre_ok >> i) & 1u ? w_pre[i] : fetch_label_word(Vv, cbx, cby, cbz);
+            // label codes, loaded a step ahead (the coincidence-free stretch needs no cache key)
+            uint32_t c_cur = fetch_label_code(Vv, cbx, cby, cbz);
             for (int k = 0; k < kk; k++) {
                 const float an = __fadd_rn(alpha, step);
                 const float nx = __fsub_rn(__fmaf_rn(an, vrx, vsx), 1.0f);
                 const float ny = __fsub_rn(__fmaf_rn(an, vry, vsy), 1.0f);
                 const float nz = __fsub_rn(__fmaf_rn(an, vrz, vsz), 1.0f);
                 const float nbx = floorf(nx), nby = floorf(ny), nbz = floorf(nz);
-                const uint32_t w_next = fetch_label_word(Vv, nbx, nby, nbz);
+                const uint32_t c_next = fetch_label_code(Vv, nbx, nby, nbz);
                 const CornerWeights cw = corner_weights(__fsub_rn(cx, cbx), __fsub_rn(cy, cby), __fsub_rn(cz, cbz));
                 const float rho = tex3D<float>(Vv.density, __fadd_rn(cx, 0.5f), __fadd_rn(cy, 0.5f), __fadd_rn(cz, 0.5f));
                 const float wr = __fmul_rn(weight, rho);
-                if (uniform_word(w_cur)) {
-                    const int L = (int)(w_cur & 15u);
+                if ((c_cur & (kCodeGeneral | 0xFF00u)) == 0u) {
+                    const int L = (int)(c_cur & 15u);
                     const float su = uniform_sum(cw);
                     if (L != cur_m) {
                         if (cur_m >= 0) store_ad<M>(ad, cur_m, cur_ad);
@@ -718,20 +716,32 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
                 } else {
                     if (cur_m >= 0) store_ad<M>(ad, cur_m, cur_ad);
                     cur_m = -1;
-                    float seg[M];
-                    label_fractions<M>(w_cur, cw, seg);
+                    if (!(c_cur & kCodeGeneral)) {
+                        const uint32_t A = c_cur & 15u, B = (c_cur >> 4) & 15u, mask = c_cur >> 8;
+                        float sA = 0.0f, sB = 0.0f;
 #pragma unroll
-                    for (int m = 0; m < M; m++) ad[m] = __fmaf_rn(wr, seg[m], ad[m]);
+                        for (int c = 0; c < 8; c++) {
+                            if ((mask >> c) & 1u)
+                                sB = __fmaf_rn(cw.xy[c & 3], cw.z[c >> 2], sB);
+                            else
+                                sA = __fmaf_rn(cw.xy[c & 3], cw.z[c >> 2], sA);
+                        }
+#pragma unroll
+                        for (int m = 0; m < M; m++)
+                            ad[m] = __fmaf_rn(wr, (uint32_t)m == A ? sA : ((uint32_t)m == B ? sB : 0.0f), ad[m]);
+                    } else {
+                        float seg[M];
+                        label_fractions<M>(fetch_label_word(Vv, cbx, cby, cbz), cw, seg);
+#pragma unroll
+                        for (int m = 0; m < M; m++) ad[m] = __fmaf_rn(wr, seg[m], ad[m]);
+                    }
                 }
                 alpha_prev = alpha;
                 alpha = an;
                 cx = nx, cy = ny, cz = nz, cbx = nbx, cby = nby, cbz = nbz;
-                w_cur = w_next;
+                c_cur = c_next;
             }
-#pragma unroll
-            for (int i = 0; i < NV; i++)
-                if (i == v) w_pre[i] = w_cur;
-            pre_ok = 1u << v;
+            pre_ok = 0u;  // the words of the next step are loaded by msample
             tracking = false;
             t += kk;
             return true;
