@@ -218,6 +218,32 @@ class Scene:
         return lib().orc_tex_point(ctypes.byref(self.sc), vol, x, y, z)
 
 
+def solid_angle(world_from_index: np.ndarray, width: int, height: int) -> np.ndarray:
+    """Solid angle (sr) of every detector pixel seen from the source, float64 [height, width].
+
+    Restates calculate_solid_angle, deepdrr/projector/project_kernel.cu:14-133: the pixel's corners
+    (u, v), (u+1, v), (u+1, v+1), (u, v+1) become source-to-corner rays r = W [u, v, 1]; the pixel
+    is split into the triangles (c0, c1, c2) and (c0, c2, c3), and each triangle's solid angle is
+    2 atan2(|a . (b x c)|, abc + (a.b) c + (a.c) b + (b.c) a), plus pi where that is negative."""
+    W = np.asarray(world_from_index, dtype=np.float64)[:3, :3]
+    v, u = np.meshgrid(np.arange(height, dtype=np.float64), np.arange(width, dtype=np.float64), indexing="ij")
+    corners = []
+    for du, dv in ((0, 0), (1, 0), (1, 1), (0, 1)):
+        cu, cv = u + du, v + dv
+        corners.append(np.stack([W[r, 0] * cu + W[r, 1] * cv + W[r, 2] for r in range(3)], -1))
+    c0, c1, c2, c3 = corners
+    mag = [np.linalg.norm(c, axis=-1) for c in corners]
+    cross = np.cross(c0, c2)
+    dot = lambda a, b: np.sum(a * b, axis=-1)  # noqa: E731
+
+    def tri(a, b, c, ma, mb, mc, numer):
+        om = 2.0 * np.arctan2(np.abs(numer), ma * mb * mc + dot(a, b) * mc + dot(a, c) * mb + dot(b, c) * ma)
+        return np.where(om < 0.0, om + np.pi, om)
+
+    return (tri(c0, c1, c2, mag[0], mag[1], mag[2], dot(c1, cross))
+            + tri(c0, c2, c3, mag[0], mag[2], mag[3], dot(c3, cross)))
+
+
 def neglog(images: np.ndarray, epsilon: float = 0.01) -> np.ndarray:
     """deepdrr/utils/image_utils.py:18-58 restated in numpy (note: it ADDS the per-image minimum)."""
     image = np.array(images, dtype=np.float32)

@@ -52,6 +52,20 @@ def oracle_scene(volumes: Sequence[Volume], proj, *, step: float = 0.1, spectrum
                         half_filter=density_dtype != "float32")
 
 
+def scene_from_record(rec, name: str, world_from_index, source_world, width: int, height: int) -> oracle.Scene:
+    """The oracle's scene for one view of a scene recorded in ``tests/golden/ref_kernel.npz``: volumes
+    named by ``{name}__volumes`` (``{key}__density`` / ``__labels`` / ``__ijk_from_world``), tables
+    and ``{name}__params`` = (step, max_ray_length, attenuate, air_index)."""
+    vols = [dict(density=rec[f"{k}__density"], labels=rec[f"{k}__labels"], ijk_from_world=rec[f"{k}__ijk_from_world"])
+            for k in (str(x) for x in rec[f"{name}__volumes"])]
+    step, max_ray_length, attenuate, air_index = (float(x) for x in rec[f"{name}__params"])
+    return oracle.Scene(vols, world_from_index, source_world, width=int(width), height=int(height), step=step,
+                        energies=rec[f"{name}__energies"], pdf=rec[f"{name}__pdf"], mu=rec[f"{name}__mu"],
+                        priorities=[int(p) for p in rec[f"{name}__priorities"]],
+                        enabled=[int(e) for e in rec[f"{name}__enabled"]], max_ray_length=max_ray_length,
+                        attenuate_outside=bool(attenuate), air_index=int(air_index))
+
+
 def quantize_density(data: np.ndarray, density_dtype: str) -> np.ndarray:
     """Densities as stored: float32 unchanged, float16 / bfloat16 rounded to nearest even."""
     if density_dtype == "float32":
