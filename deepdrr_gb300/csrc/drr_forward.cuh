@@ -64,6 +64,9 @@ struct VolConst {
     float nm1[3];                 // n - 1 per axis
     int32_t priority;
     int32_t enabled;
+    uint32_t row;          // label-table entries per row: n[0] + 1
+    uint32_t plane_bytes;  // label-table bytes per plane: 4 (n[0] + 1)(n[1] + 1), below 2^32 because
+                           // volumes are at most 16384 texels per axis (drr_volset_create)
 };
 
 struct VolPose {
@@ -180,12 +183,21 @@ __device__ __forceinline__ int clampi(int x, int lo, int hi) { return x < lo ? l
 // here because p = F (-) 1 with F = fma(alpha, r, s) a float: for |p| <= 2, p (+) 1 is exact
 // (Sterbenz), and above that 1 is a multiple of ulp(p) (up to |p| = 2^24, far outside any volume,
 // where both corners clamp to the same texel anyway). So one packed word per base suffices.
+//
+// Entry (i, j, k), 0 <= i <= n[0] etc., of a label table [(n[2]+1)][(n[1]+1)][(n[0]+1)]: the plane
+// by one widening 32 x 32 -> 64-bit multiply, the offset inside it in 32-bit arithmetic (it is
+// below (n[0]+1)(n[1]+1) <= 16385^2), the same address as ((k (n[1]+1) + j)(n[0]+1) + i) in 64 bits.
+__device__ __forceinline__ uint32_t label_entry(const uint32_t *table, const VolConst &V, int i, int j, int k) {
+    const char *plane = reinterpret_cast<const char *>(table) + (size_t)(uint32_t)k * (size_t)V.plane_bytes;
+    return __ldg(reinterpret_cast<const uint32_t *>(plane) + ((uint32_t)j * V.row + (uint32_t)i));
+}
+
 __device__ __forceinline__ uint32_t fetch_label_word(const VolConst &V, float bx, float by, float bz) {
     // packed entry of base clamp(b, -1, n-1) + 1 (bases outside behave like the clamped one)
     const int i = (int)fminf(fmaxf(bx, -1.0f), V.nm1[0]) + 1;
     const int j = (int)fminf(fmaxf(by, -1.0f), V.nm1[1]) + 1;
     const int k = (int)fminf(fmaxf(bz, -1.0f), V.nm1[2]) + 1;
-    return __ldg(V.packed + ((size_t)k * (V.n[1] + 1) + j) * (V.n[0] + 1) + i);
+    return label_entry(V.packed, V, i, j, k);
 }
 
 // The same neighbourhood as a code: A (corner 0's label) | B << 4 (the other label, or A) |
@@ -196,7 +208,7 @@ __device__ __forceinline__ uint32_t fetch_label_code(const VolConst &V, float bx
     const int i = (int)fminf(fmaxf(bx, -1.0f), V.nm1[0]) + 1;
     const int j = (int)fminf(fmaxf(by, -1.0f), V.nm1[1]) + 1;
     const int k = (int)fminf(fmaxf(bz, -1.0f), V.nm1[2]) + 1;
-    return __ldg(V.coded + ((size_t)k * (V.n[1] + 1) + j) * (V.n[0] + 1) + i);
+    return label_entry(V.coded, V, i, j, k);
 }
 
 __device__ __forceinline__ bool uniform_word(uint32_t w) { return w == (w & 15u) * 0x11111111u; }

@@ -75,6 +75,8 @@ void fill_scene(drr::SceneParams<NV> &p, const drr_volset *set, const drr_tables
         p.vol[i].hi[0] = (float)(v.ni - 0.5);
         p.vol[i].hi[1] = (float)(v.nj - 0.5);
         p.vol[i].hi[2] = (float)(v.nk - 0.5);
+        p.vol[i].row = (uint32_t)(v.ni + 1);
+        p.vol[i].plane_bytes = (uint32_t)(4u * (uint32_t)(v.ni + 1) * (uint32_t)(v.nj + 1));
         p.vol[i].priority = a.priority[i];
         p.vol[i].enabled = a.enabled[i] ? 1 : 0;
     }
