@@ -41,6 +41,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "drr_alpha.h"
 #include "drr_coincide.h"
 
@@ -57,16 +59,17 @@ constexpr int kMaxSteps = 1 << 26;      // longest march per ray; longer rays ar
 
 struct VolConst {
     cudaTextureObject_t density;  // linear filter, clamp, unnormalised coordinates
-    const uint32_t *packed;       // [(nk+1)][(nj+1)][(ni+1)] label words, see pack_labels_kernel
-    const uint32_t *coded;        // the same neighbourhoods as A | B << 4 | (corners labelled B) << 8
+    const uint32_t *packed;       // label words [(nk+1)][(nj+1)][(ni+1)] (pack_labels_kernel), at the entry of
+                                  // base (0, 0, 0): bases run from -1 to n - 1 on each axis
+    const uint32_t *coded;        // the same neighbourhoods as A | B << 4 | (corners labelled B) << 8, likewise
     int32_t n[3];                 // ni, nj, nk
     float hi[3];                  // n - 0.5 per axis (projector.py:1626-1634)
     float nm1[3];                 // n - 1 per axis
     int32_t priority;
     int32_t enabled;
-    uint32_t row;          // label-table entries per row: n[0] + 1
-    uint32_t plane_bytes;  // label-table bytes per plane: 4 (n[0] + 1)(n[1] + 1), below 2^32 because
-                           // volumes are at most 16384 texels per axis (drr_volset_create)
+    int32_t row;          // label-table entries per row: n[0] + 1
+    int32_t plane_bytes;  // label-table bytes per plane: 4 (n[0] + 1)(n[1] + 1), below 2^31 because
+                          // volumes are at most 16384 texels per axis (drr_volset_create)
 };
 
 struct VolPose {
@@ -184,19 +187,20 @@ __device__ __forceinline__ int clampi(int x, int lo, int hi) { return x < lo ? l
 // (Sterbenz), and above that 1 is a multiple of ulp(p) (up to |p| = 2^24, far outside any volume,
 // where both corners clamp to the same texel anyway). So one packed word per base suffices.
 //
-// Entry (i, j, k), 0 <= i <= n[0] etc., of a label table [(n[2]+1)][(n[1]+1)][(n[0]+1)]: the plane
-// by one widening 32 x 32 -> 64-bit multiply, the offset inside it in 32-bit arithmetic (it is
-// below (n[0]+1)(n[1]+1) <= 16385^2), the same address as ((k (n[1]+1) + j)(n[0]+1) + i) in 64 bits.
-__device__ __forceinline__ uint32_t label_entry(const uint32_t *table, const VolConst &V, int i, int j, int k) {
-    const char *plane = reinterpret_cast<const char *>(table) + (size_t)(uint32_t)k * (size_t)V.plane_bytes;
-    return __ldg(reinterpret_cast<const uint32_t *>(plane) + ((uint32_t)j * V.row + (uint32_t)i));
+// Entry of base (i, j, k), -1 <= i <= n[0] - 1 etc., of a label table [(n[2]+1)][(n[1]+1)][(n[0]+1)]
+// given at the entry of base (0, 0, 0): the plane by one widening 32 x 32 -> 64-bit multiply, the
+// offset inside it in 32-bit arithmetic (|offset| < (n[0]+1)(n[1]+1) <= 16385^2). This is the address
+// of entry ((k+1)(n[1]+1) + j+1)(n[0]+1) + i+1 of the table's start, computed in 64 bits.
+__device__ __forceinline__ uint32_t label_entry(const uint32_t *origin, const VolConst &V, int i, int j, int k) {
+    const char *plane = reinterpret_cast<const char *>(origin) + (long long)k * V.plane_bytes;
+    return __ldg(reinterpret_cast<const uint32_t *>(plane) + (j * V.row + i));
 }
 
 __device__ __forceinline__ uint32_t fetch_label_word(const VolConst &V, float bx, float by, float bz) {
-    // packed entry of base clamp(b, -1, n-1) + 1 (bases outside behave like the clamped one)
-    const int i = (int)fminf(fmaxf(bx, -1.0f), V.nm1[0]) + 1;
-    const int j = (int)fminf(fmaxf(by, -1.0f), V.nm1[1]) + 1;
-    const int k = (int)fminf(fmaxf(bz, -1.0f), V.nm1[2]) + 1;
+    // packed entry of base clamp(b, -1, n-1) (bases outside behave like the clamped one)
+    const int i = (int)fminf(fmaxf(bx, -1.0f), V.nm1[0]);
+    const int j = (int)fminf(fmaxf(by, -1.0f), V.nm1[1]);
+    const int k = (int)fminf(fmaxf(bz, -1.0f), V.nm1[2]);
     return label_entry(V.packed, V, i, j, k);
 }
 
@@ -205,9 +209,9 @@ __device__ __forceinline__ uint32_t fetch_label_word(const VolConst &V, float bx
 // itself is read). Built with the words by pack_labels_kernel.
 constexpr uint32_t kCodeGeneral = 0x80000000u;
 __device__ __forceinline__ uint32_t fetch_label_code(const VolConst &V, float bx, float by, float bz) {
-    const int i = (int)fminf(fmaxf(bx, -1.0f), V.nm1[0]) + 1;
-    const int j = (int)fminf(fmaxf(by, -1.0f), V.nm1[1]) + 1;
-    const int k = (int)fminf(fmaxf(bz, -1.0f), V.nm1[2]) + 1;
+    const int i = (int)fminf(fmaxf(bx, -1.0f), V.nm1[0]);
+    const int j = (int)fminf(fmaxf(by, -1.0f), V.nm1[1]);
+    const int k = (int)fminf(fmaxf(bz, -1.0f), V.nm1[2]);
     return label_entry(V.coded, V, i, j, k);
 }
 
@@ -446,7 +450,9 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
             cbz = floorf(cz);
             w_cur = fetch_label_code(V, cbx, cby, cbz);
         }
-        auto sample = [&](float wscale) {
+        // `half` is std::true_type for the trapezoid half-weight samples, std::false_type otherwise:
+        // a full-weight sample's weight 1 * rho is rho, so no multiply is issued for it
+        auto sample = [&](auto half) {
             const float an = __fadd_rn(alpha, step);
             const float nx = __fsub_rn(__fmaf_rn(an, rx0, sx), 1.0f);
             const float ny = __fsub_rn(__fmaf_rn(an, ry0, sy), 1.0f);
@@ -459,7 +465,7 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
             const int uni_label = (code & (kCodeGeneral | 0xFF00u)) == 0u ? (int)(code & 15u) : -1;
             const CornerWeights cw = corner_weights(fx, fy, fz);
             const float rho = tex3D<float>(V.density, __fadd_rn(px, 0.5f), __fadd_rn(py, 0.5f), __fadd_rn(pz, 0.5f));
-            const float wr = __fmul_rn(wscale, rho);
+            const float wr = decltype(half)::value ? __fmul_rn(0.5f, rho) : rho;
             if (uni_label >= 0) {
                 const float s = uniform_sum(cw);
                 if (uni_label != cur_m) {
@@ -500,16 +506,16 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
             w_cur = w_next;
         };
         if (t < t_end && t == 0) {
-            sample(0.5f);
+            sample(std::true_type{});
             ++t;
         }
         const bool last_half = t < t_end && t_end == num_steps;
         const int t_main = last_half ? t_end - 1 : t_end;
         // two samples per iteration: the loop-carried position and word then need no moves
 #pragma unroll 2
-        for (; t < t_main; ++t) sample(1.0f);
+        for (; t < t_main; ++t) sample(std::false_type{});
         if (last_half) {
-            sample(0.5f);
+            sample(std::true_type{});
             ++t;
         }
         if (cur_m >= 0) store_ad<M>(ad, cur_m, cur_ad);
@@ -699,7 +705,7 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
                     vsx = view.vol[i].s[0], vsy = view.vol[i].s[1], vsz = view.vol[i].s[2];
                 }
             const VolConst &Vv = p.vol[v];
-            const float weight = wseg;  // n = 1, full-weight samples
+            // n = 1 and full-weight samples: the weight fl(1 / 1) * rho is rho itself
             float cx = __fsub_rn(__fmaf_rn(alpha, vrx, vsx), 1.0f);
             float cy = __fsub_rn(__fmaf_rn(alpha, vry, vsy), 1.0f);
             float cz = __fsub_rn(__fmaf_rn(alpha, vrz, vsz), 1.0f);
@@ -715,7 +721,7 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
                 const uint32_t c_next = fetch_label_code(Vv, nbx, nby, nbz);
                 const CornerWeights cw = corner_weights(__fsub_rn(cx, cbx), __fsub_rn(cy, cby), __fsub_rn(cz, cbz));
                 const float rho = tex3D<float>(Vv.density, __fadd_rn(cx, 0.5f), __fadd_rn(cy, 0.5f), __fadd_rn(cz, 0.5f));
-                const float wr = __fmul_rn(weight, rho);
+                const float wr = rho;
                 if ((c_cur & (kCodeGeneral | 0xFF00u)) == 0u) {
                     const int L = (int)(c_cur & 15u);
                     const float su = uniform_sum(cw);
