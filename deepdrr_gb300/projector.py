@@ -9,8 +9,9 @@ Everything that touches the GPU goes through ``libdrr_gb300.so`` (hand-written s
 behind a C ABI); PyTorch only provides device memory and the current CUDA stream. There is no
 CPU fallback: without a CUDA device ``initialize`` raises.
 
-Not carried over: meshes (OpenGL depth peeling), scatter (deprecated in the reference, raises),
-``mode`` (stored but unused by the reference as well).
+Meshes are rasterised in CUDA (``drr_mesh_*``) instead of the reference's OpenGL depth peeling.
+Not carried over: scatter (deprecated in the reference, raises) and ``mode`` (stored but unused by
+the reference as well).
 """
 from __future__ import annotations
 
@@ -24,7 +25,7 @@ from typing import List, Optional, Sequence, Union
 import numpy as np
 
 from . import _lib, geo
-from .tables import TableSource, build_tables
+from .tables import TableSource, build_tables, configured_source
 from .mesh import Mesh
 from .volume import Volume
 
@@ -147,9 +148,13 @@ class Projector:
         self._tables_source = tables
         if len(self.all_materials) > _lib.DRR_MAX_MATERIALS:
             raise ValueError(f"at most {_lib.DRR_MAX_MATERIALS} materials are supported")
-        if tables is not None:
+        # unknown materials are rejected at construction, as the reference does (projector.py:571-577),
+        # whenever a table source is known by now (given here, set as the default or named by the
+        # environment); otherwise initialize() finds them when it builds the tables
+        source = tables if tables is not None else configured_source()
+        if source is not None:
             for mat in self.all_materials:
-                if not tables.has_material(mat):
+                if not source.has_material(mat):
                     raise ValueError(f"Material {mat} not found in material database. Please check the material name.")
         self.output_shape = None
         self.initialized = False

@@ -186,6 +186,14 @@ def default_source() -> TableSource:
     return _DEFAULT
 
 
+def configured_source() -> Optional[TableSource]:
+    """The default source if one is set or named by the environment, else None (no error)."""
+    try:
+        return default_source()
+    except RuntimeError:
+        return None
+
+
 def build_tables(spectrum: Union[str, np.ndarray], materials: Sequence[str],
                  source: Optional[TableSource] = None) -> Tuple[np.ndarray, np.ndarray, np.ndarray]:
     """(energies keV [n], pdf [n], mu [n, M]) float32 for the sorted material list ``materials``."""

@@ -49,6 +49,17 @@ def test_deprecated_and_invalid_options_raise():
         dd.Projector("not a volume")
 
 
+def test_unknown_material_raises_at_construction():
+    """projector.py:571-577: a material missing from the attenuation tables is a ValueError when the
+    projector is built (here against the default table source the test session configures)."""
+    n = 8
+    v = dd.Volume.from_parameters(np.ones((n, n, n), np.float32), {"unobtainium": np.ones((n, n, n), bool)},
+                                  origin=(0.0, 0.0, 0.0), spacing=(1.0, 1.0, 1.0))
+    with pytest.raises(ValueError, match="unobtainium"):
+        dd.Projector(v)
+    dd.Projector(uniform_cube(n, material="bone"))  # a known material passes
+
+
 def test_project_before_initialize_raises():
     p = dd.Projector(_vol())
     with pytest.raises(RuntimeError):
