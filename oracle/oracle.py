@@ -1,7 +1,7 @@
 """ctypes front end of the C oracle in ``drr_oracle.c``.
 
-TEST INFRASTRUCTURE ONLY: the tests, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
-``bench.py`` use this module as the checker. The product package never imports it.
+TEST INFRASTRUCTURE ONLY: the tests and ``__graft_entry__.smoke()`` check the product against it,
+and the CPU-baseline leg of ``bench.py`` times it. The product package never imports it.
 
 The host-side preparation follows deepdrr/projector/projector.py:802-831: the camera's
 ``world_from_index`` (3x3) and every volume's ``IJK_from_world`` (3x4) are float64 matrices cast to
