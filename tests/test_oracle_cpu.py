@@ -155,3 +155,50 @@ def test_neglog_restatement():
     np.testing.assert_allclose(out, (y - y.min()) / (y.max() - y.min()), rtol=1e-6)
     const = oracle.neglog(np.ones((2, 3, 3), dtype=np.float32))
     assert np.all(const == 0)
+
+
+def test_rays_that_miss_every_volume_are_unattenuated():
+    """A ray that crosses no volume box samples nothing (project_kernel.cu:242-244, 321-334: maxAlpha
+    stays 0, so num_steps <= 0): its photon_prob is sum(pdf) and its intensity sum(E pdf)."""
+    vol = uniform_cube(8, 1.0, material="bone")
+    proj = axis_view((0, 1, 0), sensor=(32, 4), pixel=2.0)  # ~1 mm per pixel at the cube: +-16 mm wide
+    sc = oracle_scene([vol], proj, spectrum="90KV_AL40")
+    e, pdf, _ = tables.build_tables("90KV_AL40", ["bone"], tables.NpzTables(GOLDEN_TABLES))
+    e64, p64 = e.astype(np.float64), pdf.astype(np.float64)
+    for mode, rtol in (("f64", 1e-12), ("f32", 1e-6)):
+        r = sc.project(mode)
+        for u in (0, 1, 30, 31):  # columns more than 4 mm off the axis
+            assert np.all(r["area_density"][:, :, u] == 0), (mode, u)
+            np.testing.assert_allclose(r["photon_prob"][:, u], p64.sum(), rtol=rtol)
+            np.testing.assert_allclose(r["intensity"][:, u], (e64 * p64).sum(), rtol=rtol)
+        assert np.all(r["area_density"][0, :, 15:17] > 0)  # the central columns cross the cube
+
+
+def test_max_ray_length_ends_the_march():
+    """max_ray_length caps every volume interval at alpha <= L (the slab test's upper bound,
+    project_kernel.cu:265-323): with the source 500 mm from the centre of a 16 mm cube and L = 500 mm,
+    the central ray crosses only the near half, 8 mm of it."""
+    rho, step = 1.5, 0.1
+    vol = uniform_cube(16, rho)
+    proj = axis_view((0, 1, 0), sensor=(4, 4), pixel=0.02)
+    full = oracle_scene([vol], proj, step=step)
+    cut = oracle_scene([vol], proj, step=step, max_ray_length=500.0)
+    v, u = _center_pixel(cut)
+    for mode in ("f64", "f32"):
+        ad_full = float(full.project(mode)["area_density"][0, v, u]) * 10
+        ad_cut = float(cut.project(mode)["area_density"][0, v, u]) * 10
+        assert ad_full == pytest.approx(rho * 16, abs=2 * step * rho), mode
+        assert ad_cut == pytest.approx(rho * 8, abs=2 * step * rho), mode
+
+
+def test_one_voxel_volume():
+    """A 1 x 1 x 1 volume: the box is [-0.5, 0.5] in IJK and clamp addressing returns its one texel
+    everywhere inside, so the central ray's path length is rho times the voxel's 3 mm."""
+    rho, step = 2.0, 0.1
+    vol = uniform_cube(1, rho, spacing=3.0)
+    proj = axis_view((0, 1, 0), sensor=(4, 4), pixel=0.02)
+    sc = oracle_scene([vol], proj, step=step)
+    v, u = _center_pixel(sc)
+    for mode in ("f64", "f32"):
+        ad = float(sc.project(mode)["area_density"][0, v, u]) * 10
+        assert ad == pytest.approx(rho * 3.0, abs=2 * step * rho), mode
