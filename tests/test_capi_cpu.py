@@ -43,6 +43,14 @@ def test_invalid_arguments_are_rejected_on_the_host():
     assert lib.drr_volset_create(descs, 1, 3, None, ctypes.byref(out)) == _lib.DRR_ERR_INVALID_ARGUMENT
     d.nk, d.density_type = 4, 7
     assert lib.drr_volset_create(descs, 1, 3, None, ctypes.byref(out)) == _lib.DRR_ERR_UNSUPPORTED
+    # 16384 texels per axis at most: the 3D texture limit, on which the kernels' 32-bit in-plane
+    # label-table offsets rely
+    d.density_type = 0
+    for axis in ("ni", "nj", "nk"):
+        setattr(d, axis, 16385)
+        assert lib.drr_volset_create(descs, 1, 3, None, ctypes.byref(out)) == _lib.DRR_ERR_UNSUPPORTED
+        assert "16384" in lib.drr_last_error().decode()
+        setattr(d, axis, 4)
     assert lib.drr_tables_create(None, None, None, 3, 3, None, ctypes.byref(out)) == _lib.DRR_ERR_INVALID_ARGUMENT
     args = _lib.drr_project_args()
     assert lib.drr_project(None, None, ctypes.byref(args), None) == _lib.DRR_ERR_INVALID_ARGUMENT
