@@ -39,7 +39,7 @@ DRR_FLAG_PERSISTENT = 1 << 2
 EXPORTED_SYMBOLS = (
     "drr_volset_create", "drr_volset_destroy", "drr_volset_set_density", "drr_ingest_hu", "drr_tables_create", "drr_tables_destroy",
     "drr_project", "drr_project_adjoint", "drr_graph_create", "drr_graph_set_views", "drr_graph_launch", "drr_graph_destroy",
-    "drr_autotune", "drr_mesh_hits", "drr_mesh_area_density", "drr_add_noise", "drr_poisson_sample", "drr_neglog", "drr_neglog_noalloc", "drr_clip_upper", "drr_last_error", "drr_version",
+    "drr_autotune", "drr_mesh_hits", "drr_mesh_area_density", "drr_add_noise", "drr_poisson_sample", "drr_neglog", "drr_neglog_noalloc", "drr_clip_upper", "drr_texture_rate", "drr_last_error", "drr_version",
 )
 
 
@@ -60,8 +60,19 @@ class drr_volume_desc(ctypes.Structure):
     ]
 
 
-class drr_project_args(ctypes.Structure):
+class _Sized(ctypes.Structure):
+    """An argument struct whose first field, struct_size, must hold its own size (the library
+    rejects any other value); instances are created with it filled in."""
+
+    def __init__(self, *args, **kwargs):
+        super().__init__(*args, **kwargs)
+        if "struct_size" not in kwargs:
+            self.struct_size = ctypes.sizeof(self)
+
+
+class drr_project_args(_Sized):
     _fields_ = [
+        ("struct_size", ctypes.c_uint32),
         ("width", ctypes.c_int32), ("height", ctypes.c_int32),
         ("step", ctypes.c_float), ("max_ray_length", ctypes.c_float),
         ("air_index", ctypes.c_int32), ("flags", ctypes.c_uint32),
@@ -86,8 +97,9 @@ class drr_mesh_desc(ctypes.Structure):
     ]
 
 
-class drr_adjoint_args(ctypes.Structure):
+class drr_adjoint_args(_Sized):
     _fields_ = [
+        ("struct_size", ctypes.c_uint32),
         ("area_density", ctypes.c_void_p), ("grad_intensity", ctypes.c_void_p),
         ("grad_photon_prob", ctypes.c_void_p), ("grad_area_density", ctypes.c_void_p),
         ("grad_density", ctypes.c_void_p), ("grad_pose", ctypes.c_void_p),
@@ -161,6 +173,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     lib.drr_neglog_noalloc.restype = st
     lib.drr_clip_upper.argtypes = [vp, ctypes.c_int64, ctypes.c_float, vp]
     lib.drr_clip_upper.restype = st
+    lib.drr_texture_rate.argtypes = [i32, vp, ctypes.POINTER(ctypes.c_double)]
+    lib.drr_texture_rate.restype = st
     lib.drr_last_error.argtypes = []
     lib.drr_last_error.restype = ctypes.c_char_p
     lib.drr_version.argtypes = []

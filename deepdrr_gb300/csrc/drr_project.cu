@@ -238,8 +238,20 @@ drr_status project_persistent(drr_volset *set, const drr_tables *tab, const drr_
     return DRR_OK;
 }
 
+// The caller's struct must be this library's drr_project_args: checked before any other field is read.
+drr_status check_struct_size(const drr_project_args *args) {
+    if (!args) return fail(DRR_ERR_INVALID_ARGUMENT, "drr_project: NULL args");
+    if (args->struct_size != sizeof(drr_project_args))
+        return fail(DRR_ERR_INVALID_ARGUMENT, "drr_project: args->struct_size is " + std::to_string(args->struct_size) +
+                                                  ", this library's drr_project_args has " +
+                                                  std::to_string(sizeof(drr_project_args)) + " bytes");
+    return DRR_OK;
+}
+
 drr_status validate(const drr_volset *set, const drr_tables *tables, const drr_project_args *args) {
-    if (!set || !tables || !args) return fail(DRR_ERR_INVALID_ARGUMENT, "drr_project: NULL handle or args");
+    const drr_status sz = check_struct_size(args);
+    if (sz != DRR_OK) return sz;
+    if (!set || !tables) return fail(DRR_ERR_INVALID_ARGUMENT, "drr_project: NULL handle");
     const drr_project_args &a = *args;
     if (a.width < 1 || a.height < 1) return fail(DRR_ERR_INVALID_ARGUMENT, "drr_project: empty detector");
     if ((int64_t)a.width * a.height > (int64_t)1 << 28)
@@ -548,7 +560,14 @@ drr_status ensure_point_texture(drr::Volume &v) {
 extern "C" drr_status drr_project_adjoint(drr_volset *set, const drr_tables *tables, const drr_project_args *args,
                                           const drr_adjoint_args *adj, void *stream) {
     drr::set_last_error("");
-    if (!set || !tables || !args || !adj) return fail(DRR_ERR_INVALID_ARGUMENT, "drr_project_adjoint: NULL argument");
+    const drr_status sz = check_struct_size(args);
+    if (sz != DRR_OK) return sz;
+    if (!adj) return fail(DRR_ERR_INVALID_ARGUMENT, "drr_project_adjoint: NULL adjoint args");
+    if (adj->struct_size != sizeof(drr_adjoint_args))
+        return fail(DRR_ERR_INVALID_ARGUMENT, "drr_project_adjoint: adj->struct_size is " +
+                                                  std::to_string(adj->struct_size) + ", this library's drr_adjoint_args has " +
+                                                  std::to_string(sizeof(drr_adjoint_args)) + " bytes");
+    if (!set || !tables) return fail(DRR_ERR_INVALID_ARGUMENT, "drr_project_adjoint: NULL argument");
     if (set->n_volumes != 1) return fail(DRR_ERR_UNSUPPORTED, "drr_project_adjoint: one volume only");
     if (args->flags & DRR_FLAG_ATTENUATE_OUTSIDE)
         return fail(DRR_ERR_UNSUPPORTED, "drr_project_adjoint: DRR_FLAG_ATTENUATE_OUTSIDE is not differentiated");

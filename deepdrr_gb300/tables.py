@@ -18,8 +18,9 @@ DeepDRR checkout), or is set with ``set_default_source``.
 """
 from __future__ import annotations
 
-import importlib.util
+import ast
 import os
+import re
 from pathlib import Path
 from typing import Dict, List, Optional, Sequence, Tuple, Union
 
@@ -151,13 +152,35 @@ class DeepDRRDataTables(TableSource):
 
     def spectrum(self, name: str) -> np.ndarray:
         if self._spectra is None:
-            spec = importlib.util.spec_from_file_location("_deepdrr_spectral_data", self.spectral_path)
-            mod = importlib.util.module_from_spec(spec)
-            spec.loader.exec_module(mod)
-            self._spectra = dict(mod.spectrums)
+            self._spectra = parse_spectral_data(self.spectral_path.read_text())
         if name not in self._spectra:
             raise KeyError(f"unrecognized spectrum: {name}")
         return np.asarray(self._spectra[name], dtype=np.float64)
+
+
+_ARRAY_RE = re.compile(r"^(\w+)\s*=\s*np\.array\(\s*(\[.*?\])\s*\)", re.S | re.M)
+_NAME_RE = re.compile(r"'([^']+)'\s*:\s*(\w+)")
+
+
+def parse_spectral_data(text: str) -> Dict[str, np.ndarray]:
+    """The spectra of deepdrr/projector/spectral_data.py, read as data without running the module:
+    each ``NAME = np.array([[eV, weight], ...])`` literal (spectral_data.py:7, 99, 251) and the
+    ``spectrums = {'60KV_AL35': NAME, ...}`` map (spectral_data.py:463-467). The numbers are parsed
+    as Python float literals, which gives the float64 values numpy builds from them."""
+    arrays = {m.group(1): np.asarray(ast.literal_eval(m.group(2)), dtype=np.float64)
+              for m in _ARRAY_RE.finditer(text)}
+    start = text.find("spectrums")
+    if start < 0:
+        raise ValueError("no `spectrums` map in the spectral data")
+    body = text[start:text.index("}", start)]
+    out = {}
+    for key, var in _NAME_RE.findall(body):
+        if var not in arrays:
+            raise ValueError(f"spectrum {key!r} names an unknown array {var}")
+        out[key] = arrays[var]
+    if not out:
+        raise ValueError("the `spectrums` map is empty")
+    return out
 
 
 _DEFAULT: Optional[TableSource] = None

@@ -114,8 +114,13 @@ enum {
     DRR_FLAG_PERSISTENT = 1 << 2         /* one persistent launch for all views (dynamic (view, tile) scheduling) */
 };
 
-/* Arguments of one drr_project call: `n_views` views of the same volume set. */
+/* Arguments of one drr_project call: `n_views` views of the same volume set. `struct_size` must be
+ * sizeof(drr_project_args) as the caller's binding lays the struct out (e.g.
+ * `drr_project_args a = {sizeof(drr_project_args)};`); any other value is rejected with
+ * DRR_ERR_INVALID_ARGUMENT before any other field is read, so a binding whose copy of this struct
+ * has drifted from the library's fails loudly instead of having fields read past its end. */
 typedef struct {
+    uint32_t struct_size;           /* sizeof(drr_project_args) */
     int32_t width, height;          /* detector size in pixels */
     float step;                     /* ray step in world units (mm), Projector(step=...) */
     float max_ray_length;           /* <= 0: unlimited; projector.py:641-650 */
@@ -227,8 +232,10 @@ typedef struct {
 drr_status drr_autotune(drr_volset *set, const drr_tables *tables, const drr_project_args *args, int32_t max_views,
                         void *stream, drr_tune_result *best);
 
-/* Upstream gradients and gradient outputs of drr_project_adjoint. Device pointers. */
+/* Upstream gradients and gradient outputs of drr_project_adjoint. Device pointers. `struct_size`
+ * must be sizeof(drr_adjoint_args), as for drr_project_args. */
 typedef struct {
+    uint32_t struct_size;           /* sizeof(drr_adjoint_args) */
     const float *area_density;      /* [n_views][n_materials][H][W]: drr_project's area_density for the
                                        same args, or NULL to recompute it (stream-ordered scratch) */
     const float *grad_intensity;    /* [n_views][H][W] dL/d(intensity), or NULL */
@@ -270,8 +277,8 @@ drr_status drr_poisson_sample(const float *lambda, int64_t n, uint64_t seed, flo
 /* In-place negative-log transform of `n_views` float32 images of `pixels_per_view` pixels each,
  * on `stream`: per view x += min(x) + epsilon; x = -log(x); x = (x - min) / (max - min), and every
  * view becomes 0 if any view is constant. Replaces deepdrr/utils/image_utils.py:18-58 (`_neglog`,
- * applied by Projector.project at projector.py:700-702). Uses 12 bytes per view of stream-ordered
- * scratch (cudaMallocAsync). */
+ * applied by Projector.project at projector.py:700-702). Uses 12 bytes per view (plus 4) of
+ * stream-ordered scratch (cudaMallocAsync). */
 drr_status drr_neglog(float *images, int32_t n_views, int64_t pixels_per_view, float epsilon, void *stream);
 
 /* drr_neglog for callers that cannot allocate device memory. This entry point has no counterpart
@@ -279,15 +286,25 @@ drr_status drr_neglog(float *images, int32_t n_views, int64_t pixels_per_view, f
  * in which cudaMalloc or cudaFree would stall the device, and pipelines that record their work
  * into CUDA graphs while forbidding allocation calls all need a transform that allocates nothing.
  * It computes exactly what drr_neglog computes but keeps its scratch (3 words per view) in one
- * fixed device array inside the library, 48 KiB that every GPU loading the library keeps until the
- * process exits; n_views above 4096 is rejected with DRR_ERR_UNSUPPORTED. The first call on a
- * device looks up that array's device address (make it before any stream capture). All calls
- * share the array: calls whose work overlaps on the GPU, on any streams, race and must be ordered
- * by the caller. Each call resets the words it uses before reading them. */
+ * fixed device array inside the library, about 48 KiB that every GPU loading the library keeps until
+ * the process exits; n_views above 4096 is rejected with DRR_ERR_UNSUPPORTED. The first call in a
+ * CUDA context (on each device, and again after a cudaDeviceReset or under another driver context)
+ * looks up that array's device address in the context and caches it: make that first call before
+ * any stream capture. All calls share the array: calls whose work overlaps on the GPU, on any
+ * streams, race and must be ordered by the caller. Each call resets the words it uses before
+ * reading them. */
 drr_status drr_neglog_noalloc(float *images, int32_t n_views, int64_t pixels_per_view, float epsilon, void *stream);
 
 /* In-place min(x, upper) over `n` floats: Projector(intensity_upper_bound=...), projector.py:697-698. */
 drr_status drr_clip_upper(float *images, int64_t n, float upper, void *stream);
+
+/* Measurement aid with no counterpart in the reference: the rate, in fetches per second, at which
+ * this GPU's texture units return trilinear-filtered samples of an L1-resident 3D texture of
+ * `density_type` (DRR_DENSITY_F32 or DRR_DENSITY_F16), timed on `stream` with the forward kernel's
+ * launch shape (best of five launches). Every sample of the forward march makes one such fetch, so
+ * this is the ceiling of its sample rate. Synchronous; holds a 16^3 texture and a small output
+ * buffer for the duration of the call. */
+drr_status drr_texture_rate(int32_t density_type, void *stream, double *fetches_per_second);
 
 /* Human-readable description of the last error raised on this host thread ("" if none). */
 const char *drr_last_error(void);

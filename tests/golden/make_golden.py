@@ -1,8 +1,9 @@
 """Generate the golden spectrum / mass-attenuation tables from the reference implementation.
 
-Run in a container where the DeepDRR sources are available (default ``/root/reference``):
+Run where the DeepDRR sources are available (``--reference``, default: the DEEPDRR_REFERENCE
+environment variable, as oracle/build_ref.py resolves it):
 
-    python tests/golden/make_golden.py [--reference /root/reference]
+    python tests/golden/make_golden.py [--reference PATH]
 
 It imports the reference's own ``deepdrr.material`` package and ``deepdrr/projector/spectral_data.py``
 (without the top-level ``deepdrr/__init__``, which needs CuPy and an OpenGL stack) and writes
@@ -27,6 +28,12 @@ from pathlib import Path
 
 import numpy as np
 
+ROOT = Path(__file__).resolve().parents[2]
+if str(ROOT) not in sys.path:
+    sys.path.insert(0, str(ROOT))
+
+from oracle.build_ref import default_reference  # noqa: E402
+
 MATERIALS = ["air", "soft tissue", "bone", "titanium", "lung", "muscle", "iron", "blood"]
 
 
@@ -49,7 +56,7 @@ def _load_reference(ref: Path):
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=str(default_reference()))
     ap.add_argument("--out", default=str(Path(__file__).with_name("tables.npz")))
     args = ap.parse_args()
     Material, spectrums = _load_reference(Path(args.reference))

@@ -6,10 +6,11 @@ import numpy as np
 import pytest
 
 from deepdrr_gb300 import tables
+from oracle.build_ref import default_reference
 
 from helpers import GOLDEN_TABLES
 
-REFERENCE = Path("/root/reference")
+REFERENCE = default_reference()
 SPECTRA = ["60KV_AL35", "90KV_AL40", "120KV_AL43"]
 MATS = ["air", "soft tissue", "bone", "titanium", "lung", "muscle", "iron", "blood"]
 
