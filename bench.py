@@ -1,24 +1,42 @@
 #!/usr/bin/env python
 """Benchmark of the DRR forward projector on one GB300 (or N independent replicas).
 
-Workload (the production-size plain forward): a seeded 512 x 512 x 400 float32 CT phantom at
-0.8 x 0.8 x 1.0 mm (body, lungs, spine, ribs, titanium; materials air / bone / soft tissue /
-titanium), a 1536 x 1536 detector at 0.194 mm, SDD 1020 mm, 32 seeded poses (point in a 100 mm
-ball, direction in a 30 degree cone, source-to-point fraction 0.5-0.9), 90 kVp spectrum
+Headline workload (the production-size plain forward): a seeded 512 x 512 x 400 float32 CT
+phantom at 0.8 x 0.8 x 1.0 mm (body, lungs, spine, ribs, titanium; materials air / bone / soft
+tissue / titanium), a 1536 x 1536 detector at 0.194 mm, SDD 1020 mm, 32 seeded poses (point in a
+100 mm ball, direction in a 30 degree cone, source-to-point fraction 0.5-0.9), 90 kVp spectrum
 (151 bins), step 0.1 mm. One *step* renders the 32 views one launch per view.
 
-  value  projections/s of the kernels with the volume resident in HBM (CUDA events on the
-         launching stream, K timed steps after W warm-up steps, max over ranks)
-  e2e    projections/s through the public API ``Projector.project(view)`` returning a host
-         numpy image after GPU neglog (device->host copy of every image inside the timed region)
+  value     projections/s of the kernels with the volume resident in HBM (CUDA events on the
+            launching stream, K timed steps after W warm-up steps, max over ranks)
+  e2e       projections/s through the public API ``Projector.project(view)`` returning a host
+            numpy image after GPU neglog (device->host copy of every image inside the timed region)
+  roofline  the forward kernel against its binding bound, the texture unit's filtered-fetch rate
+            (one trilinear fetch per sample), measured live by drr_texture_rate; the HBM figures
+            (compulsory bytes, ncu DRAM traffic) are in ``roofline_hbm``
+
+Baselines in the same line: ``reference_kernel`` times the reference's own projectKernel (compiled
+from the reference sources, driven as _render_single drives it) on the same GPU and views;
+``cpu_baseline`` times the oracle's float64 C restatement of its stepping rule on the host cores.
+
+Unless ``--no-extra`` (or N > 1), the line also carries the other configurations, each measured in
+this run with 3 warm-up and 3 timed steps:
+  c1        128^3 phantom, one 256^2 view at 120 kVp (ours and the reference kernel)
+  batched   3 volumes (512x512x400 CT, 256^3 phantom, 96x96x64 implant), 256 views at 384^2: one
+            graph-captured persistent launch against plain launches, a per-view Projector.project
+            loop, and the reference kernel
+  adjoint   256^3 phantom, 64 views at 256^2: forward and forward + backward ms/view, memory
+  half      512^3 CT, 32 views at 1536^2, 120 kVp, stored as float32 / float16 / bfloat16: speed,
+            resident bytes, error against the float64 oracle
 
 ``--impl reference`` times the oracle's float64 C restatement of the reference stepping rule on
-all host cores over a bounded ray sample (the reference projector itself only runs on a GPU
-through CuPy + EGL, which this machine does not have).
+all host cores over a bounded ray sample (the reference projector itself only runs on a GPU,
+through CuPy and an EGL context, which this machine does not have).
 """
 from __future__ import annotations
 
 import argparse
+import hashlib
 import json
 import os
 import statistics
@@ -35,6 +53,7 @@ METRIC = "DRR projections/s & Gsamples/s (512³ CT, 1536² det); fwd+adjoint ms/
 TABLES = ROOT / "tests" / "golden" / "tables.npz"
 PEAKS = ROOT / "MEASURED_PEAKS.json"
 TRAFFIC_FILE = ROOT / "profiles" / "forward_ct512_det1536_dram.txt"
+SUB_WARMUP, SUB_STEPS = 3, 3
 
 
 def parse_args():
@@ -47,10 +66,11 @@ def parse_args():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--density-dtype", default="float32", choices=["float32", "float16", "bfloat16"])
     ap.add_argument("--workload", default="ct", choices=["ct", "ct512", "multi", "adjoint"],
-                    help="ct: 512x512x400 CT, 90 kVp (default); ct512: 512^3 CT, 120 kVp; "
-                         "multi: 3 volumes, 256 views at 384^2, one graph-captured persistent launch")
+                    help="ct: 512x512x400 CT, 90 kVp (default, with the other configurations as sub-objects); "
+                         "ct512 / multi / adjoint: one configuration alone")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-extra", action="store_true", help="headline only: no sub-objects, no reference kernel")
     ap.add_argument("--small", action="store_true", help="a 128^3 / 256^2 workload for quick checks")
     return ap.parse_args()
 
@@ -76,6 +96,7 @@ class ClockSampler:
             self.thread.start()
         except FileNotFoundError:
             self.proc = None
+        return self
 
     def _read(self):
         for line in self.proc.stdout:
@@ -131,6 +152,121 @@ def workload(args, rank: int, world: int = 1):
     return vols, projs, kw, name
 
 
+# ---------------------------------------------------------------- helpers -----------------------
+
+def material_list(vols):
+    return sorted({m for v in vols for m in v.materials[0]})
+
+
+def remapped_labels(vol, mats):
+    """Labels as indices into the sorted material list (projector.py:1495-1519)."""
+    import numpy as np
+
+    names, seg = vol.materials
+    lut = np.zeros(max(names.values()) + 1, dtype=np.uint8)
+    for n, i in names.items():
+        lut[i] = mats.index(n)
+    return lut[seg]
+
+
+def scene_volumes(vols, mats):
+    return [dict(density=v.data, labels=remapped_labels(v, mats), ijk_from_world=v.ijk_from_world.data) for v in vols]
+
+
+def source_sha() -> str:
+    """Hash of the kernel sources, to tell whether a saved ncu figure still describes this build."""
+    h = hashlib.sha256()
+    for p in sorted((ROOT / "deepdrr_gb300" / "csrc").glob("*.cu*")) + sorted((ROOT / "deepdrr_gb300" / "csrc").glob("*.h")):
+        h.update(p.name.encode())
+        h.update(p.read_bytes())
+    return h.hexdigest()[:16]
+
+
+def read_profile_figures() -> dict:
+    out = {}
+    if TRAFFIC_FILE.exists():
+        for ln in TRAFFIC_FILE.read_text().splitlines():
+            if ln.startswith("#") or ":" not in ln:
+                continue
+            key, _, val = ln.partition(":")
+            val = val.strip()
+            try:
+                out[key.strip()] = float(val)
+            except ValueError:
+                out[key.strip()] = val
+    return out
+
+
+def texture_rate(density_dtype: str) -> float:
+    import ctypes
+
+    import torch
+
+    from deepdrr_gb300 import _lib
+
+    rate = ctypes.c_double(0.0)
+    kind = _lib.DRR_DENSITY_F32 if density_dtype == "float32" else _lib.DRR_DENSITY_F16
+    _lib.check(_lib.load().drr_texture_rate(kind, ctypes.c_void_p(torch.cuda.current_stream().cuda_stream),
+                                            ctypes.byref(rate)))
+    return rate.value
+
+
+def tex_roofline(samples_per_s: float, density_dtype: str, peak_fetches: float) -> dict:
+    from deepdrr_gb300 import metrics
+
+    b = metrics.BYTES_PER_SAMPLE[density_dtype]
+    achieved = samples_per_s * b / 1e9
+    peak = peak_fetches * b / 1e9
+    return {"bound": "tex", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "bytes_per_sample": b, "peak_fetches_per_s": peak_fetches,
+            "note": "sampled bytes (8 density + 8 label texels per sample) at the forward's sample rate, against the "
+                    "same bytes at the texture unit's measured trilinear-fetch rate (drr_texture_rate, one fetch per "
+                    "sample, measured in this run): frac = samples/s / filtered fetches/s"}
+
+
+def timed_events(fn, warmup: int, steps: int, stream) -> float:
+    """Mean ms per call of fn, CUDA events on `stream`, after `warmup` untimed calls."""
+    import torch
+
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        fn()
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def reference_kernel_times(vols, projs, kw, *, views: int, repeats: int = 2) -> dict:
+    """The reference's own projectKernel on `views` of these views: mean kernel ms per view (CUDA
+    events, `repeats` launches per view after one untimed launch) and the host time of one whole
+    _render_single sequence per view (geometry upload, launch, both read-backs, transposes)."""
+    from deepdrr_gb300 import geo, tables
+    from oracle import ref_kernel
+
+    mats = material_list(vols)
+    if not ref_kernel.available(len(vols), len(mats)):
+        return {"unavailable": "reference cubins not built (no reference sources where this tree was built)"}
+    e, pdf, mu = tables.build_tables(kw["spectrum"], mats, tables.NpzTables(TABLES))
+    rs = ref_kernel.RefScene(scene_volumes(vols, mats), energies=e, pdf=pdf, mu=mu)
+    ms, wall = [], []
+    try:
+        for pr in projs[:views]:
+            W, s, w, h = geo.view_arrays(pr)
+            r = rs.project(W, s, w, h, step=kw["step"], outputs=False, repeats=repeats, wall=True)
+            ms.append(r["ms"])
+            wall.append(r["wall_ms"])
+    finally:
+        rs.close()
+    return {"views": len(ms), "ms_per_view": statistics.mean(ms), "projections_per_s": 1000.0 / statistics.mean(ms),
+            "render_single_wall_ms_per_view": statistics.mean(wall),
+            "source": "deepdrr/projector/project_kernel.cu:135-650 compiled for sm_103a with the reference's -D "
+                      "macros, launched as projector.py:759-774 (8x8 blocks, one launch per view)"}
+
+
 def cpu_baseline(vols, projs, kw, stride: int = 16, threads: int = 0):
     """Oracle float64 restatement of the reference stepping rule on a ray sample (every `stride`-th
     row and column of the first view), all host cores. Returns (projections/s, cores, sample)."""
@@ -140,18 +276,11 @@ def cpu_baseline(vols, projs, kw, stride: int = 16, threads: int = 0):
     from oracle import oracle
 
     src = tables.NpzTables(TABLES)
-    mats = sorted({m for v in vols for m in v.materials[0]})
+    mats = material_list(vols)
     e, pdf, mu = tables.build_tables(kw["spectrum"], mats, src)
     W, s, w, h = geo.view_arrays(projs[0])
-    vlist = []
-    for v in vols:
-        names, seg = v.materials
-        lut = np.zeros(max(names.values()) + 1, dtype=np.uint8)
-        for n, i in names.items():
-            lut[i] = mats.index(n)
-        vlist.append(dict(density=v.data, labels=lut[seg], ijk_from_world=v.ijk_from_world.data))
-    sc = oracle.Scene(vlist, W, s, width=w, height=h, step=kw["step"], energies=e, pdf=pdf, mu=mu,
-                      max_ray_length=-4.0)
+    sc = oracle.Scene(scene_volumes(vols, mats), W, s, width=w, height=h, step=kw["step"], energies=e, pdf=pdf,
+                      mu=mu, max_ray_length=-4.0)
     vv, uu = np.meshgrid(np.arange(0, h, stride), np.arange(0, w, stride), indexing="ij")
     ids = (vv * w + uu).ravel().astype(np.int64)
     cores = threads or os.cpu_count() or 1
@@ -164,11 +293,20 @@ def cpu_baseline(vols, projs, kw, stride: int = 16, threads: int = 0):
                              f"{dt:.2f} s, float64, extrapolated to whole views"
 
 
+def free_memory_bytes() -> int:
+    import torch
+
+    torch.cuda.synchronize()
+    return int(torch.cuda.mem_get_info()[0])
+
+
+# ---------------------------------------------------------------- --impl reference --------------
+
 def run_reference(args, rank: int, world: int):
     if rank != 0:
         return
     vols, projs, kw, name = workload(args, 0)
-    stride = 2 if not args.small else 1  # about 10 s of float64 work per step on 16 host cores
+    stride = 4 if not args.small else 1  # about 2.5 s of float64 work per step on 16 host cores
     vals, dts = [], []
     for k in range(args.warmup + args.steps):
         t0 = time.perf_counter()
@@ -190,74 +328,102 @@ def run_reference(args, rank: int, world: int):
     print(json.dumps(line), flush=True)
 
 
-def run_batched(args, rank, world, local):
-    """Many views of several volumes: K graph replays of one persistent launch over all views
-    (autotuned launch shape) against the same views rendered with one plain launch per view."""
+# ---------------------------------------------------------------- configurations ----------------
+
+def phase_c1(args, local) -> dict:
+    """128^3 phantom, one 256^2 view at 120 kVp: ours (plain launch) and the reference kernel."""
+    import numpy as np
     import torch
 
     import deepdrr_gb300 as dd
-    from deepdrr_gb300 import metrics, tables
+    from deepdrr_gb300 import geo, metrics, phantoms, tables
+    from oracle import ref_kernel
 
-    torch.cuda.set_device(local)
-    vols, projs, kw, name = workload(args, rank)
+    vols, projs, kw = phantoms.workload_simple(seed=args.seed, views=1)
     p = dd.Projector(vols, spectrum=kw["spectrum"], step=kw["step"], tables=tables.NpzTables(TABLES), neglog=False,
-                     density_dtype=args.density_dtype, cuda_device_id=local)
+                     cuda_device_id=local)
     p.initialize()
     stream = torch.cuda.current_stream()
+    ms = timed_events(lambda: p.project_tensors(projs[0]), 20, 50, stream)
+    ours = p.project_tensors(projs[0])["intensity"][0].cpu().numpy()
+    samples = float(metrics.count_samples(vols, projs, kw["step"], -4.0, device=f"cuda:{local}").sum())
+    p.free()
+    out = {"workload": "simple128^3_det256_1view_120kV", "ms_per_view": ms, "projections_per_s": 1000.0 / ms,
+           "gsamples_per_s": samples / (ms / 1000.0) / 1e9, "timing": "20 warm-up + 50 timed launches"}
+    mats = material_list(vols)
+    if ref_kernel.available(1, len(mats)):
+        e, pdf, mu = tables.build_tables(kw["spectrum"], mats, tables.NpzTables(TABLES))
+        rs = ref_kernel.RefScene(scene_volumes(vols, mats), energies=e, pdf=pdf, mu=mu)
+        W, s, w, h = geo.view_arrays(projs[0])
+        r = rs.project(W, s, w, h, step=kw["step"], repeats=50, wall=True)
+        rs.close()
+        rel = np.abs(ours.astype(np.float64) - r["intensity"]) / np.abs(r["intensity"].astype(np.float64))
+        out["reference_kernel"] = {"ms_per_view": r["ms"], "projections_per_s": 1000.0 / r["ms"],
+                                   "render_single_wall_ms_per_view": r["wall_ms"], "speedup": r["ms"] / ms,
+                                   "max_rel_intensity_vs_ours": float(rel.max())}
+    return out
+
+
+def phase_batched(args, local) -> dict:
+    """Three volumes, 256 views at 384^2: graph-captured persistent launch vs plain launches, a
+    per-view Projector.project loop and the reference kernel."""
+    import torch
+
+    import deepdrr_gb300 as dd
+    from deepdrr_gb300 import metrics, phantoms, tables
+
+    vols, projs, kw = phantoms.workload_multi(seed=args.seed, views=256)
     n = len(projs)
     W, H = projs[0].sensor_width, projs[0].sensor_height
+    free0 = free_memory_bytes()
+    p = dd.Projector(vols, spectrum=kw["spectrum"], step=kw["step"], tables=tables.NpzTables(TABLES), neglog=True,
+                     cuda_device_id=local)
+    p.initialize()
+    resident = free0 - free_memory_bytes()
+    stream = torch.cuda.current_stream()
     samples = float(metrics.count_samples(vols, projs, kw["step"], -4.0, device=f"cuda:{local}").sum())
-    shape = p.autotune(*projs, max_views=min(n, 64), cache=False)
+    shape = p.autotune(*projs, max_views=64, cache=False)
     graph = p.capture(*projs, launch=shape)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(local).start()
+    ms_graph = timed_events(lambda: graph.launch(), SUB_WARMUP, SUB_STEPS, stream)
+    clk = clocks.stop()
+    ms_plain = timed_events(lambda: [p.project_tensors(pr) for pr in projs], SUB_WARMUP, SUB_STEPS, stream)
+    graph.close()
 
-    def timed(fn):
-        for _ in range(args.warmup):
+    def wall(fn):
+        fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(SUB_STEPS):
             fn()
         torch.cuda.synchronize()
-        e0.record(stream)
-        for _ in range(args.steps):
-            fn()
-        e1.record(stream)
-        e1.synchronize()
-        return e0.elapsed_time(e1) / args.steps
+        return (time.perf_counter() - t0) / SUB_STEPS
 
-    clocks = ClockSampler(local)
-    clocks.start()
-    ms_graph = timed(lambda: graph.launch())
-    clk = clocks.stop()
-    ms_persistent = timed(lambda: p.project_tensors(*projs, persistent=True, launch=shape))
-    ms_plain = timed(lambda: [p.project_tensors(pr) for pr in projs])
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        p.project(*projs)
-    torch.cuda.synchronize()
-    e2e = n * args.steps / (time.perf_counter() - t0)
-    graph.close()
+    e2e_batched = wall(lambda: p.project(*projs))
+    e2e_loop = wall(lambda: [p.project(pr) for pr in projs])
     p.free()
-    value = n / (ms_graph / 1000.0)
-    line = {
-        "metric": METRIC, "value": value, "unit": "projections/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms_graph, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded phantoms, seeded poses)",
-        "config": {"workload": name, "views_per_step": n, "detector": [W, H], "launch": "persistent, CUDA graph",
-                   "autotuned_shape": shape, "l2": "inputs larger than L2 (three volume textures, 0.9 GB)"},
-        "gsamples_per_s": samples / (ms_graph / 1000.0) / 1e9,
-        "persistent_projections_per_s": n / (ms_persistent / 1000.0),
-        "plain_projections_per_s": n / (ms_plain / 1000.0),
-        "speedup_vs_plain": ms_plain / ms_graph,
-        "gpu_launches": 1, "clocks": clk,
-        "e2e": {"value": e2e, "unit": "projections/s", "h2d_bytes_per_step": n * (9 + 3 + 12 * len(vols)) * 8,
-                "d2h_bytes_per_step": n * W * H * 4},
-    }
-    if rank == 0:
-        print(json.dumps(line), flush=True)
+    del graph, p
+    torch.cuda.empty_cache()
+    out = {"workload": "multi3_ct512x512x400+256^3+96x96x64_det384_256views_90kV", "views_per_step": n,
+           "graph_projections_per_s": n / (ms_graph / 1000.0), "plain_projections_per_s": n / (ms_plain / 1000.0),
+           "speedup_graph_vs_plain": ms_plain / ms_graph, "gsamples_per_s": samples / (ms_graph / 1000.0) / 1e9,
+           "autotuned_shape": shape, "resident_bytes": resident, "clocks": clk,
+           "e2e": {"batched_projections_per_s": n / e2e_batched, "per_view_loop_projections_per_s": n / e2e_loop,
+                   "speedup_batched_vs_per_view_loop": e2e_loop / e2e_batched,
+                   "note": "Projector.project(*views) -> host numpy [256, 384, 384] after GPU neglog, against "
+                           "[Projector.project(v) for v in views], the reference's serial pattern "
+                           "(projector.py:679-685)", "d2h_bytes_per_step": n * W * H * 4},
+           "timing": f"{SUB_WARMUP} warm-up + {SUB_STEPS} timed steps of 256 views"}
+    ref = reference_kernel_times(vols, projs, kw, views=8)
+    if "ms_per_view" in ref:
+        ref["speedup_graph"] = ref["ms_per_view"] / (ms_graph / n)
+        ref["speedup_plain"] = ref["ms_per_view"] / (ms_plain / n)
+    out["reference_kernel"] = ref
+    return out
 
 
-def run_adjoint(args, rank, world, local):
-    """2D/3D registration step: differentiable forward of all views, MSE against target images
-    rendered at a perturbed pose, backward to the density volume and the 6-DoF pose. Timed with
-    the area densities stored for the backward pass and with them recomputed there."""
+def phase_adjoint(args, local) -> dict:
+    """2D/3D registration step on the 256^3 phantom, 64 views at 256^2."""
     import numpy as np
     import torch
 
@@ -265,8 +431,7 @@ def run_adjoint(args, rank, world, local):
     from deepdrr_gb300 import autograd, tables
     from deepdrr_gb300.phantoms import workload_adjoint
 
-    torch.cuda.set_device(local)
-    vols, projs, kw = workload_adjoint(seed=args.seed + rank, views=args.views if args.views != 32 else 64)
+    vols, projs, kw = workload_adjoint(seed=args.seed, views=64)
     vol = vols[0]
     n = len(projs)
     W, H = projs[0].sensor_width, projs[0].sensor_height
@@ -289,55 +454,89 @@ def run_adjoint(args, rank, world, local):
         return loss
 
     def timed(fn):
-        for _ in range(args.warmup):
+        for _ in range(SUB_WARMUP):
             fn()
         torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda.reset_peak_memory_stats()
         base = torch.cuda.memory_allocated()
-        e0.record(stream)
-        for _ in range(args.steps):
-            fn()
-        e1.record(stream)
-        e1.synchronize()
-        return e0.elapsed_time(e1) / args.steps, torch.cuda.max_memory_allocated() - base
+        ms = timed_events(fn, 0, SUB_STEPS, stream)
+        return ms, torch.cuda.max_memory_allocated() - base
 
-    clocks = ClockSampler(local)
-    clocks.start()
+    clocks = ClockSampler(local).start()
     ms_fwd, _ = timed(lambda: step(False, backward=False))
     ms_stored, mem_stored = timed(lambda: step(False))
     ms_recompute, mem_recompute = timed(lambda: step(True))
     clk = clocks.stop()
-    # gradient sanity: one step's pose gradient points from the target pose back to zero
     d = rho.detach().requires_grad_()
     pose = torch.zeros(6, dtype=torch.float64, requires_grad=True)
     out = autograd.project(p, *projs, density=d, pose=pose, center=center)
     ((out["intensity"] - target) ** 2).mean().backward()
     g = pose.grad.numpy()
     cos = float(-(g @ kw["target_pose"]) / (np.linalg.norm(g) * np.linalg.norm(kw["target_pose"]) + 1e-30))
-    p.free()
     M = len(p.all_materials)
-    line = {
-        "metric": METRIC, "value": ms_stored / n, "unit": "ms/view (fwd+bwd)", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_stored, "higher_is_better": False,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded phantom, seeded poses)",
-        "config": {"workload": f"adjoint_phantom{vol.shape[0]}^3_det{W}_{n}views_90kV", "views_per_step": n,
-                   "detector": [W, H], "materials": M, "loss": "MSE vs target at a pose perturbed <=5 mm / 5 deg",
-                   "gradients": "density (f32 volume) + 6-DoF pose",
-                   "l2": "density texture 64 MB + 64 MB gradient volume; outputs re-read once"},
-        "fwd_ms_per_view": ms_fwd / n,
-        "fwd_bwd_ms_per_view_stored": ms_stored / n,
-        "fwd_bwd_ms_per_view_recompute": ms_recompute / n,
-        "bwd_over_fwd": (ms_stored - ms_fwd) / ms_fwd,
-        "fwd_bwd_over_fwd": ms_stored / ms_fwd,
-        "memory_bytes": {"stored_peak": mem_stored, "recompute_peak": mem_recompute,
-                         "area_density_held": n * M * W * H * 4},
-        "pose_grad_cosine_to_target_direction": cos,
-        "gpu_launches": 2 * n // 32 + 2, "clocks": clk,
-    }
-    if rank == 0:
-        print(json.dumps(line), flush=True)
+    p.free()
+    return {"workload": f"adjoint_phantom{vol.shape[0]}^3_det{W}_{n}views_90kV", "views_per_step": n,
+            "loss": "MSE vs target at a pose perturbed <=5 mm / 5 deg", "gradients": "density (f32 volume) + 6-DoF pose",
+            "fwd_ms_per_view": ms_fwd / n, "fwd_bwd_ms_per_view_stored": ms_stored / n,
+            "fwd_bwd_ms_per_view_recompute": ms_recompute / n, "fwd_bwd_over_fwd": ms_stored / ms_fwd,
+            "fwd_bwd_over_fwd_recompute": ms_recompute / ms_fwd,
+            "memory_bytes": {"stored_peak": mem_stored, "recompute_peak": mem_recompute,
+                             "area_density_held": n * M * W * H * 4},
+            "pose_grad_cosine_to_target_direction": cos, "clocks": clk,
+            "timing": f"{SUB_WARMUP} warm-up + {SUB_STEPS} timed steps of 64 views"}
 
+
+def phase_half(args, local) -> dict:
+    """512^3 CT, 32 views at 1536^2, 120 kVp: float32 / float16 / bfloat16 density storage."""
+    import numpy as np
+    import torch
+
+    import deepdrr_gb300 as dd
+    from deepdrr_gb300 import metrics, phantoms, tables
+
+    vols, projs, kw = phantoms.workload_ct(seed=args.seed, views=32, shape=(512, 512, 512), spectrum="120KV_AL43")
+    stream = torch.cuda.current_stream()
+    samples = float(metrics.count_samples(vols, projs, kw["step"], -4.0, device=f"cuda:{local}").sum())
+    _, _, sample = cpu_baseline(vols, projs, kw, stride=8)
+    ids, ref = cpu_baseline.last
+    ids_t = torch.from_numpy(ids).to(f"cuda:{local}")
+    out = {"workload": "ct512x512x512_det1536_32views_120kV", "views_per_step": len(projs),
+           "error_sample": sample.replace("extrapolated to whole views", "first view"),
+           "timing": f"{SUB_WARMUP} warm-up + {SUB_STEPS} timed steps of 32 views per storage type"}
+    for dt in ("float32", "float16", "bfloat16"):
+        free0 = free_memory_bytes()
+        p = dd.Projector(vols, spectrum=kw["spectrum"], step=kw["step"], tables=tables.NpzTables(TABLES), neglog=False,
+                         density_dtype=dt, cuda_device_id=local)
+        p.initialize()
+        resident = free0 - free_memory_bytes()
+        clocks = ClockSampler(local).start()
+        ms = timed_events(lambda: [p.project_tensors(pr) for pr in projs], SUB_WARMUP, SUB_STEPS, stream)
+        clk = clocks.stop()
+        got = p.project_tensors(projs[0])["intensity"][0].flatten()[ids_t].double().cpu().numpy()
+        rel = np.abs(got - ref) / np.maximum(np.abs(ref), 1e-12)
+        p.free()
+        del p
+        torch.cuda.empty_cache()
+        out[dt] = {"projections_per_s": len(projs) / (ms / 1000.0), "ms_per_view": ms / len(projs),
+                   "gsamples_per_s": samples / (ms / 1000.0) / 1e9, "resident_bytes": resident,
+                   "max_rel_intensity_vs_float64": float(rel.max()), "mean_rel_intensity_vs_float64": float(rel.mean()),
+                   "clocks": clk}
+    return out
+
+
+# ---------------------------------------------------------------- standalone configurations -----
+
+def run_single(args, rank, world, local):
+    import torch
+
+    torch.cuda.set_device(local)
+    fn = {"multi": phase_batched, "adjoint": phase_adjoint, "ct512": phase_half}[args.workload]
+    res = fn(args, local)
+    if rank == 0:
+        print(json.dumps({"metric": METRIC, "workload": args.workload, "n_gpus": world, **res}), flush=True)
+
+
+# ---------------------------------------------------------------- the headline line -------------
 
 def main():
     args = parse_args()
@@ -346,10 +545,8 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         return run_reference(args, rank, world)
-    if args.workload == "multi":
-        return run_batched(args, rank, world, local)
-    if args.workload == "adjoint":
-        return run_adjoint(args, rank, world, local)
+    if args.workload != "ct" and not args.small:
+        return run_single(args, rank, world, local)
 
     import numpy as np
     import torch
@@ -364,12 +561,15 @@ def main():
         import torch.distributed as dist
 
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    extra = not args.no_extra and world == 1 and not args.small
     vols, projs, kw, name = workload(args, rank, world)
     src = tables.NpzTables(TABLES)
     nviews = len(projs)
+    free0 = free_memory_bytes()
     p = dd.Projector(vols, spectrum=kw["spectrum"], step=kw["step"], tables=src, neglog=True,
                      density_dtype=args.density_dtype, cuda_device_id=local)
     p.initialize()
+    resident = free0 - free_memory_bytes()
     W, H = projs[0].sensor_width, projs[0].sensor_height
     samples = metrics.count_samples(vols, projs, kw["step"], -4.0, device=f"cuda:{local}")
     samples_per_step = float(samples.sum())
@@ -388,8 +588,7 @@ def main():
     for _ in range(args.warmup):
         step_plain()
     barrier()
-    clocks = ClockSampler(local)
-    clocks.start()
+    clocks = ClockSampler(local).start()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
@@ -405,15 +604,7 @@ def main():
     gsamples = samples_per_step * world * args.steps / (ms / 1000.0) / 1e9
 
     # batched: all views of a step in one library call
-    for _ in range(2):
-        p.project_tensors(*projs)
-    barrier()
-    e0.record(stream)
-    for _ in range(args.steps):
-        p.project_tensors(*projs)
-    e1.record(stream)
-    e1.synchronize()
-    ms_b = e0.elapsed_time(e1) / args.steps
+    ms_b = timed_events(lambda: p.project_tensors(*projs), 2, args.steps, stream)
 
     # end to end through the public API (host numpy out, neglog on the GPU)
     e2e = None
@@ -431,25 +622,30 @@ def main():
         e2e = {"value": nviews * args.steps * world / dt, "unit": "projections/s",
                "h2d_bytes_per_step": geometry_bytes, "d2h_bytes_per_step": nviews * W * H * 4}
 
-    # roofline of the forward kernel: compulsory HBM bytes per launch (one view) over its duration
+    # roofline: the texture unit's filtered-fetch rate (binding), and the HBM figures beside it
     peaks = json.loads(PEAKS.read_text()) if PEAKS.exists() else {}
-    hbm_peak = peaks.get("hbm_gbs", 6800.0)
-    comp = metrics.compulsory_bytes(vols, W, H, args.density_dtype)
+    hbm_peak = peaks.get("hbm_gbs")
+    hbm_src = "of measured (MEASURED_PEAKS.json hbm_gbs)"
+    if hbm_peak is None:
+        hbm_peak, hbm_src = 6800.0, "of fallback (6.8 TB/s)"
+    peak_fetches = texture_rate(args.density_dtype)
     launch_s = ms_per_step / 1000.0 / nviews
-    achieved = comp / launch_s / 1e9
-    traffic = tex_pipe = l1_hit = l2_hit = None
-    if TRAFFIC_FILE.exists():
-        for ln in TRAFFIC_FILE.read_text().splitlines():
-            key, _, val = ln.partition(":")
-            if key == "dram_bytes_per_launch":
-                traffic = float(val)
-            elif key == "tex_pipe_pct":
-                tex_pipe = float(val)
-            elif key == "l1tex_hit_pct":
-                l1_hit = float(val)
-            elif key == "l2_hit_pct":
-                l2_hit = float(val)
-    sampled_bytes = samples_per_step / nviews * metrics.BYTES_PER_SAMPLE[args.density_dtype]
+    comp = metrics.compulsory_bytes(vols, W, H, args.density_dtype)
+    prof = read_profile_figures()
+    sha = source_sha()
+    stale = prof.get("source_sha") != sha
+    roofline = tex_roofline(samples_per_step / nviews / launch_s, args.density_dtype, peak_fetches)
+    roofline["traffic"] = prof.get("dram_bytes_per_launch")
+    roofline["traffic_note"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch, "
+                                f"profiles/{TRAFFIC_FILE.name}" + (" (captured on an earlier build of the kernels)"
+                                                                    if stale else " (this build)"))
+    roofline["tex_pipe_pct_ncu"] = prof.get("tex_pipe_pct")
+    roofline_hbm = {"bound": "hbm", "achieved": comp / launch_s / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                    "frac": comp / launch_s / 1e9 / hbm_peak, "traffic": prof.get("dram_bytes_per_launch"),
+                    "algorithmic_bytes_per_launch": comp, "l2_hit_pct_ncu": prof.get("l2_hit_pct"),
+                    "l1tex_hit_pct_ncu": prof.get("l1tex_hit_pct"),
+                    "note": "compulsory bytes (each voxel's density + label once, plus the output images) per view, "
+                            f"peak {hbm_src}; not the binding bound: the volume is read from HBM about once per view"}
     line = {
         "metric": METRIC, "value": value, "unit": "projections/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -463,18 +659,14 @@ def main():
                    "l2": "inputs larger than L2 (volume textures > 129 MB)"},
         "gsamples_per_s": gsamples,
         "samples_per_view": samples_per_step / nviews,
+        "ms_per_view": ms_per_step / nviews,
         "batched_projections_per_s": nviews / (ms_b / 1000.0),
+        "resident_bytes": resident,
         "gpu_launches": nviews * args.steps,
         "clocks": clk,
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "traffic": traffic,
-                     "algorithmic_bytes_per_launch": comp,
-                     "note": "compulsory bytes (each voxel's density+label once, plus output images) per view; "
-                             "peak = measured copy bandwidth of MEASURED_PEAKS.json"},
-        "sampled": {"bytes_per_launch": sampled_bytes, "gb_per_s": sampled_bytes / launch_s / 1e9,
-                    "tex_pipe_pct_of_peak_ncu": tex_pipe, "l1tex_hit_pct_ncu": l1_hit, "l2_hit_pct_ncu": l2_hit,
-                    "note": "texel bytes the march reads per view (40 B/sample at float32), served by L1/TEX; "
-                            "texture-pipe utilisation from the ncu capture in profiles/"},
+        "roofline": roofline,
+        "roofline_hbm": roofline_hbm,
+        "kernel_source_sha": sha,
         "e2e": e2e,
     }
     if rank == 0 and not args.no_cpu_baseline:
@@ -487,7 +679,33 @@ def main():
         rel = np.abs(got.double().cpu().numpy() - ref) / np.maximum(np.abs(ref), 1e-12)
         line["error_vs_float64"] = {"max_rel_intensity": float(rel.max()), "mean_rel_intensity": float(rel.mean()),
                                     "rays": int(ids.shape[0])}
+    if extra:
+        # ours on the same views the reference kernel is timed on, kernel time only
+        n_ref = min(4, nviews)
+        ms_ours = timed_events(lambda: [p.project_tensors(pr) for pr in projs[:n_ref]], 1, 2, stream) / n_ref
     p.free()
+    del p
+    torch.cuda.empty_cache()
+    if extra:
+        ref = reference_kernel_times(vols, projs, kw, views=n_ref)
+        if "ms_per_view" in ref:
+            ref["ours_ms_per_view_same_views"] = ms_ours
+            ref["speedup"] = ref["ms_per_view"] / ms_ours
+            if e2e is not None:
+                ref["speedup_e2e"] = ref["render_single_wall_ms_per_view"] / (1000.0 / e2e["value"])
+                ref["e2e_note"] = ("reference: geometry upload + kernel + read-back and transpose of intensity and "
+                                   "photon_prob (its host neglog not counted); ours: Projector.project(view) with "
+                                   "GPU neglog and the image read back")
+        line["reference_kernel"] = ref
+        del vols, projs
+        line["c1"] = phase_c1(args, local)
+        line["batched"] = phase_batched(args, local)
+        line["batched"]["peak_fetches_per_s"] = peak_fetches
+        line["batched"]["roofline"] = tex_roofline(line["batched"]["gsamples_per_s"] * 1e9, "float32", peak_fetches)
+        line["adjoint"] = phase_adjoint(args, local)
+        line["half"] = phase_half(args, local)
+        line["half"]["roofline_float16"] = tex_roofline(line["half"]["float16"]["gsamples_per_s"] * 1e9, "float16",
+                                                        texture_rate("float16"))
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist is not None:

@@ -5,6 +5,7 @@
 //   image  = -log(image)
 //   image  = (image - min) / (max - min)  per view; if any view is constant, every view becomes 0
 // All arithmetic is float32 like the reference's numpy float32 arrays.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -79,14 +80,21 @@ __global__ void neglog_log(float *__restrict__ img, int64_t npix, float epsilon,
     }
 }
 
-__global__ void neglog_scale(float *__restrict__ img, int64_t npix, int n_views, const unsigned int *keys) {
-    __shared__ int any_constant;
-    if (threadIdx.x == 0) {
-        int c = 0;
-        for (int v = 0; v < n_views; v++) c |= (keys[v * 3 + 1] == keys[v * 3 + 2]);
-        any_constant = c;
-    }
+// keys[3 * n_views] = 1 if any view is constant after the log (its min and max agree), else 0:
+// one block, so the scaling pass reads one word instead of every view's keys.
+__global__ void neglog_flag(unsigned int *keys, int n_views) {
+    __shared__ int any;
+    if (threadIdx.x == 0) any = 0;
     __syncthreads();
+    int c = 0;
+    for (int v = threadIdx.x; v < n_views; v += blockDim.x) c |= (keys[v * 3 + 1] == keys[v * 3 + 2]);
+    if (c) atomicOr(&any, 1);
+    __syncthreads();
+    if (threadIdx.x == 0) keys[3 * n_views] = (unsigned int)any;
+}
+
+__global__ void neglog_scale(float *__restrict__ img, int64_t npix, int n_views, const unsigned int *keys) {
+    const bool any_constant = keys[3 * n_views] != 0u;
     const int view = blockIdx.y;
     float *x = img + (int64_t)view * npix;
     const float lo = kfloat(keys[view * 3 + 1]);
@@ -117,7 +125,7 @@ extern "C" drr_status drr_neglog(float *images, int32_t n_views, int64_t pixels_
     }
     cudaStream_t s = (cudaStream_t)stream;
     unsigned int *keys = nullptr;
-    cudaError_t e = cudaMallocAsync((void **)&keys, sizeof(unsigned int) * 3 * (size_t)n_views, s);
+    cudaError_t e = cudaMallocAsync((void **)&keys, sizeof(unsigned int) * (3 * (size_t)n_views + 1), s);
     if (e != cudaSuccess) {
         drr::set_last_error(std::string("drr_neglog: cudaMallocAsync: ") + cudaGetErrorString(e));
         return DRR_ERR_OUT_OF_MEMORY;
@@ -126,6 +134,7 @@ extern "C" drr_status drr_neglog(float *images, int32_t n_views, int64_t pixels_
     neglog_init<<<(n_views + 255) / 256, 256, 0, s>>>(keys, n_views);
     neglog_min<<<grid, kThreads, 0, s>>>(images, pixels_per_view, keys);
     neglog_log<<<grid, kThreads, 0, s>>>(images, pixels_per_view, epsilon, keys);
+    neglog_flag<<<1, kThreads, 0, s>>>(keys, n_views);
     neglog_scale<<<grid, kThreads, 0, s>>>(images, pixels_per_view, n_views, keys);
     e = cudaGetLastError();
     cudaFreeAsync(keys, s);
@@ -141,44 +150,79 @@ extern "C" drr_status drr_neglog(float *images, int32_t n_views, int64_t pixels_
 // Some hosts cannot let a library allocate device memory: a renderer or simulator that owns the
 // allocator and pre-budgets every byte, a real-time loop where cudaMalloc/cudaFree would
 // synchronise the device, or a CUDA-graph-based pipeline that forbids allocation calls while it
-// records. For them this entry point keeps its 12 bytes per view of scratch in a fixed file-scope
-// device array instead of allocating it. Every GPU that loads the library holds the array
-// (kNoAllocMaxViews * 12 bytes = 48 KiB) until the process exits.
+// records. For them this entry point keeps its 12 bytes per view of scratch (plus one flag word) in
+// a fixed file-scope device array instead of allocating it. Every GPU that loads the library holds
+// the array (kNoAllocMaxViews * 12 + 256 bytes, about 48 KiB) until the process exits.
 namespace {
 
 constexpr int kNoAllocMaxViews = 4096;
-constexpr int kNoAllocMaxDevices = 64;
+constexpr int kNoAllocCacheEntries = 64;
 
-static __device__ __align__(256) unsigned int g_neglog_scratch[3 * kNoAllocMaxViews];
+static __device__ __align__(256) unsigned int g_neglog_scratch[3 * kNoAllocMaxViews + 64];
+
+// The array's device address differs per CUDA context (each context loads its own copy of the
+// module), so it is cached per context, keyed by the driver's context ID, which no later context
+// reuses: a cudaDeviceReset, or a caller that makes its own driver context current, gets a new
+// lookup instead of a stale address. The driver's context queries are reached through the
+// runtime's entry-point table, so the library does not link libcuda.
+using CtxGetCurrentFn = CUresult (*)(CUcontext *);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long *);
 
 std::mutex g_scratch_mutex;
-unsigned int *g_scratch_address[kNoAllocMaxDevices] = {};
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+CtxGetIdFn g_ctx_get_id = nullptr;
+bool g_ctx_queries_resolved = false;
+struct ScratchEntry {
+    unsigned long long ctx_id;
+    unsigned int *ptr;
+};
+ScratchEntry g_scratch_cache[kNoAllocCacheEntries];
+int g_scratch_cached = 0;
 
-// Device address of g_neglog_scratch on the current device. In host code the array's name is only
-// a host-side stand-in, so the address is looked up once per device (with that device current)
-// and cached.
+drr_status scratch_fail(const char *what, cudaError_t e) {
+    drr::set_last_error(std::string("drr_neglog_noalloc: ") + what + ": " + cudaGetErrorString(e));
+    return DRR_ERR_CUDA;
+}
+
+// ID of the context current on this thread, or 0 if none is (or the driver cannot say).
+unsigned long long current_context_id() {
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (g_ctx_get_current && g_ctx_get_id && g_ctx_get_current(&ctx) == CUDA_SUCCESS && ctx &&
+        g_ctx_get_id(ctx, &id) == CUDA_SUCCESS)
+        return id;
+    return 0;
+}
+
+// Device address of g_neglog_scratch in the current context. In host code the array's name is
+// only a host-side stand-in, so the address is looked up with cudaGetSymbolAddress, once per
+// context (the first call on each device, with that device current), and cached.
 drr_status scratch_address(unsigned int **out) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) {
-        drr::set_last_error(std::string("drr_neglog_noalloc: cudaGetDevice: ") + cudaGetErrorString(e));
-        return DRR_ERR_CUDA;
-    }
-    if (dev < 0 || dev >= kNoAllocMaxDevices) {
-        drr::set_last_error("drr_neglog_noalloc: device ordinal beyond the supported range");
-        return DRR_ERR_UNSUPPORTED;
-    }
     std::lock_guard<std::mutex> lock(g_scratch_mutex);
-    if (g_scratch_address[dev] == nullptr) {
-        unsigned int *ptr = nullptr;
-        e = cudaGetSymbolAddress((void **)&ptr, g_neglog_scratch);
-        if (e != cudaSuccess || ptr == nullptr) {
-            drr::set_last_error(std::string("drr_neglog_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-            return DRR_ERR_CUDA;
-        }
-        g_scratch_address[dev] = ptr;
+    if (!g_ctx_queries_resolved) {
+        cudaDriverEntryPointQueryResult q;
+        void *fn = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            g_ctx_get_current = reinterpret_cast<CtxGetCurrentFn>(fn);
+        fn = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            g_ctx_get_id = reinterpret_cast<CtxGetIdFn>(fn);
+        g_ctx_queries_resolved = true;
     }
-    *out = g_scratch_address[dev];
+    unsigned long long id = current_context_id();
+    for (int i = 0; id != 0 && i < g_scratch_cached; i++)
+        if (g_scratch_cache[i].ctx_id == id) {
+            *out = g_scratch_cache[i].ptr;
+            return DRR_OK;
+        }
+    unsigned int *ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress((void **)&ptr, g_neglog_scratch);  // makes the primary context current
+    if (e != cudaSuccess || ptr == nullptr) return scratch_fail("cudaGetSymbolAddress", e);
+    if (id == 0) id = current_context_id();
+    if (id != 0 && g_scratch_cached < kNoAllocCacheEntries) g_scratch_cache[g_scratch_cached++] = {id, ptr};
+    *out = ptr;
     return DRR_OK;
 }
 
@@ -205,6 +249,7 @@ extern "C" drr_status drr_neglog_noalloc(float *images, int32_t n_views, int64_t
     neglog_init<<<(n_views + 255) / 256, 256, 0, s>>>(keys, n_views);
     neglog_min<<<grid, kThreads, 0, s>>>(images, pixels_per_view, keys);
     neglog_log<<<grid, kThreads, 0, s>>>(images, pixels_per_view, epsilon, keys);
+    neglog_flag<<<1, kThreads, 0, s>>>(keys, n_views);
     neglog_scale<<<grid, kThreads, 0, s>>>(images, pixels_per_view, n_views, keys);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {

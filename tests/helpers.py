@@ -94,3 +94,22 @@ def rel_err(a, b, floor: float = 0.0):
     a = np.asarray(a, dtype=np.float64)
     b = np.asarray(b, dtype=np.float64)
     return np.abs(a - b) / np.maximum(np.abs(b), floor)
+
+
+class DeltaTables(tables.TableSource):
+    """One 1 keV bin with pdf 1 and mu/rho = 1 for material `name`, 0 otherwise: then
+    photon_prob = exp(-area_density[name]), which exposes the reference kernel's path lengths."""
+
+    SPECTRUM = np.array([[1000.0, 1.0]])
+
+    def __init__(self, name):
+        self.name = name
+
+    def spectrum(self, name):
+        return self.SPECTRUM
+
+    def has_material(self, material):
+        return True
+
+    def mu_over_rho(self, material, energies_kev, spectrum_name=None):
+        return np.full(np.shape(energies_kev), 1.0 if material == self.name else 0.0, dtype=np.float32)

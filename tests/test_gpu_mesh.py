@@ -162,3 +162,82 @@ def test_subtractive_mesh_carves_the_volume():
     # centre pixels cross the 8 mm box along its depth (magnification 2: the box spans ~20 pixels)
     assert abs(diff[16, 16] - 8.0) <= 0.25
     assert np.all(np.abs(diff[:4]) < 1e-6) and np.all(np.abs(diff[:, :4]) < 1e-6)
+
+
+# ---------------------------------------------------------------- against the reference kernel --
+
+def _mesh_buffers(p, proj):
+    """The projector's own rasterisation for one view: subtractive hit lists [L][H][W][K] and the
+    per-slot additive integrals [S][H][W] (what drr_project reads), with the slots' materials."""
+    keep = []
+    desc = p._mesh_desc(keep)
+    W, s, w, h = geo.view_arrays(proj)
+    wfi = np.ascontiguousarray(W[None], dtype=np.float64)
+    src = np.ascontiguousarray(np.asarray(s)[None], dtype=np.float64)
+    L, K = p.mesh_layers, p.max_mesh_hits
+    ha = torch.empty((L, h, w, K), dtype=torch.float32, device="cuda")
+    hf = torch.empty((L, h, w, K), dtype=torch.int8, device="cuda")
+    lib = _lib.load()
+    _lib.check(lib.drr_mesh_hits(ctypes.byref(desc), w, h, wfi.ctypes.data, src.ctypes.data, K, ha.data_ptr(),
+                                 hf.data_ptr(), None))
+    S = len(p.mesh_materials)
+    out = torch.empty((1, S, h, w), dtype=torch.float32, device="cuda")
+    p._mesh_fill(desc, wfi, src, w, h, out, (ha, hf))
+    torch.cuda.synchronize()
+    mats = np.asarray([p.all_materials.index(m) for m in p.mesh_materials], dtype=np.int32)
+    return ha.cpu().numpy(), hf.cpu().numpy(), out[0].cpu().numpy(), mats
+
+
+def test_forward_consumes_meshes_like_the_reference_kernel():
+    """The march's use of subtractive hit lists (project_kernel.cu:498-521: a sample inside any
+    layer adds nothing) and of additive integrals (project_kernel.cu:569-579: added per material
+    after the step scaling, before the division by 10), against the reference kernel compiled with
+    MESH_ADDITIVE_ENABLED=1 and given the same hit lists and integrals in its own layouts
+    ([2][H][W][32] hits with every layer valid; [2][n_mesh_materials][H][W][2] integrals, layer 0
+    holding ours with a balanced crossing count). Intensity within 1e-4, path lengths within 1e-5
+    relative (read out through one-bin spectra) plus read-out noise."""
+    from oracle import ref_kernel
+
+    from helpers import DeltaTables, labels_for
+
+    vol = volume_from_hu(simple_phantom_hu(40, seed=2))
+    c = vol.center_in_world
+    tool = Mesh.icosphere(6.0, center=c + np.array([3.0, 0.0, 2.0]), material="titanium")
+    cut = Mesh.box((12.0, 9.0, 10.0), center=c + np.array([-4.0, 1.0, -1.0]), material="titanium", additive=False,
+                   subtractive=True, layer=0)
+    cut2 = Mesh.icosphere(4.0, center=c + np.array([5.0, -3.0, 0.0]), subdivisions=2, material="titanium",
+                          additive=False, subtractive=True, layer=1)
+    proj = random_views(1, c, seed=9, sphere_mm=2.0, sensor_size=(48, 40), pixel_size=2.0,
+                        fraction_range=(0.5, 0.6))[0]
+    golden = tables.NpzTables(GOLDEN_TABLES)
+    W, s, w, h = geo.view_arrays(proj)
+    with dd.Projector([vol, tool, cut, cut2], spectrum="90KV_AL40", tables=golden, neglog=False, step=0.1) as p:
+        mats = p.all_materials
+        if not ref_kernel.available(1, len(mats), mesh_additive=True):
+            pytest.skip("reference cubins not built (no reference sources where this tree was built)")
+        assert p.mesh_layers == ref_kernel.MESH_LAYERS and p.max_mesh_hits == ref_kernel.MAX_MESH_HITS
+        ha, hf, add, slot_mats = _mesh_buffers(p, proj)
+    assert (hf[0] != 0).any() and (hf[1] != 0).any() and (add > 0).sum() > 50
+    additive = np.zeros((ref_kernel.MESH_LAYERS, len(slot_mats), h, w, 2), np.float32)
+    additive[0, :, :, :, 0] = add
+    vols_ref = [dict(density=vol.data, labels=labels_for(vol, mats), ijk_from_world=vol.ijk_from_world.data)]
+    for spectrum, src, m in [("90KV_AL40", golden, None)] + [(DeltaTables.SPECTRUM, DeltaTables(n), i)
+                                                             for i, n in enumerate(mats)]:
+        with dd.Projector([vol, tool, cut, cut2], spectrum=spectrum, tables=src, neglog=False, step=0.1) as p:
+            got = {k: v[0].cpu().numpy() for k, v in p.project_tensors(proj, area_density=True).items()}
+        e, pdf, mu = tables.build_tables(spectrum, mats, src)
+        rs = ref_kernel.RefScene(vols_ref, energies=e, pdf=pdf, mu=mu, mesh_additive=True)
+        ref = rs.project(W, s, w, h, step=0.1, hit_alpha=ha, hit_facing=hf, layer_valid=np.ones(2, np.int8),
+                         additive=additive, unique_materials=slot_mats)
+        rs.close()
+        if m is None:
+            rel = np.abs(got["intensity"].astype(np.float64) - ref["intensity"]) / ref["intensity"]
+            print(f"meshes: intensity max rel {rel.max():.3g}")
+            assert rel.max() <= 1e-4
+        else:
+            pp32 = ref["photon_prob"]
+            ad_ref = -np.log(pp32.astype(np.float64))
+            noise = 2.0 * np.spacing(pp32).astype(np.float64) / pp32
+            err = np.abs(got["area_density"][m].astype(np.float64) - ad_ref)
+            print(f"meshes: path length of {mats[m]}: max abs err {err.max():.3g} (max {ad_ref.max():.4g} g/cm^2)")
+            assert np.all(err <= 1e-5 * ad_ref + noise), (mats[m], err.max())

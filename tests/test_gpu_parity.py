@@ -24,28 +24,9 @@ from deepdrr_gb300.phantoms import (ct_phantom, implant_volume, random_rigid, ra
                                     volume_from_hu)
 from oracle import oracle, ref_kernel
 
-from helpers import GOLDEN_TABLES, labels_for, material_list, oracle_scene, rel_err, uniform_cube
+from helpers import GOLDEN_TABLES, DeltaTables, labels_for, material_list, oracle_scene, rel_err, uniform_cube
 
 pytestmark = pytest.mark.gpu
-
-
-class DeltaTables(tables.TableSource):
-    """One 1 keV bin with pdf 1 and mu/rho = 1 for material `name`, 0 otherwise: then
-    photon_prob = exp(-area_density[name]), which exposes the reference kernel's path lengths."""
-
-    SPECTRUM = np.array([[1000.0, 1.0]])
-
-    def __init__(self, name):
-        self.name = name
-
-    def spectrum(self, name):
-        return self.SPECTRUM
-
-    def has_material(self, material):
-        return True
-
-    def mu_over_rho(self, material, energies_kev, spectrum_name=None):
-        return np.full(np.shape(energies_kev), 1.0 if material == self.name else 0.0, dtype=np.float32)
 
 
 def run_product(volumes, projs, *, spectrum="90KV_AL40", source=None, priorities=None, attenuate=False,
