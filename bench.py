@@ -11,9 +11,11 @@ tissue / titanium), a 1536 x 1536 detector at 0.194 mm, SDD 1020 mm, 32 seeded p
             launching stream, K timed steps after W warm-up steps, max over ranks)
   e2e       projections/s through the public API ``Projector.project(view)`` returning a host
             numpy image after GPU neglog (device->host copy of every image inside the timed region)
-  roofline  the forward kernel against its binding bound, the texture unit's filtered-fetch rate
-            (one trilinear fetch per sample), measured live by drr_texture_rate; the HBM figures
-            (compulsory bytes, ncu DRAM traffic) are in ``roofline_hbm``
+  roofline  the forward kernel against the measured HBM copy bandwidth: compulsory bytes per
+            launch over its duration, with the ncu DRAM traffic of one launch beside it. The kernel
+            is bound by instruction issue and the texture pipe, not HBM: ``tex_pipe`` carries the
+            texture-pipe and issue utilisation of the latest ncu capture, marked stale when the
+            kernel sources changed since
 
 Baselines in the same line: ``reference_kernel`` times the reference's own projectKernel (compiled
 from the reference sources, driven as _render_single drives it) on the same GPU and views;
@@ -197,33 +199,6 @@ def read_profile_figures() -> dict:
     return out
 
 
-def texture_rate(density_dtype: str) -> float:
-    import ctypes
-
-    import torch
-
-    from deepdrr_gb300 import _lib
-
-    rate = ctypes.c_double(0.0)
-    kind = _lib.DRR_DENSITY_F32 if density_dtype == "float32" else _lib.DRR_DENSITY_F16
-    _lib.check(_lib.load().drr_texture_rate(kind, ctypes.c_void_p(torch.cuda.current_stream().cuda_stream),
-                                            ctypes.byref(rate)))
-    return rate.value
-
-
-def tex_roofline(samples_per_s: float, density_dtype: str, peak_fetches: float) -> dict:
-    from deepdrr_gb300 import metrics
-
-    b = metrics.BYTES_PER_SAMPLE[density_dtype]
-    achieved = samples_per_s * b / 1e9
-    peak = peak_fetches * b / 1e9
-    return {"bound": "tex", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "bytes_per_sample": b, "peak_fetches_per_s": peak_fetches,
-            "note": "sampled bytes (8 density + 8 label texels per sample) at the forward's sample rate, against the "
-                    "same bytes at the texture unit's measured trilinear-fetch rate (drr_texture_rate, one fetch per "
-                    "sample, measured in this run): frac = samples/s / filtered fetches/s"}
-
-
 def timed_events(fn, warmup: int, steps: int, stream) -> float:
     """Mean ms per call of fn, CUDA events on `stream`, after `warmup` untimed calls."""
     import torch
@@ -294,9 +269,12 @@ def cpu_baseline(vols, projs, kw, stride: int = 16, threads: int = 0):
 
 
 def free_memory_bytes() -> int:
+    """Free device memory, with torch's cache of freed blocks (the staging tensors of
+    Projector.initialize) returned first, so that differences are what the library holds."""
     import torch
 
     torch.cuda.synchronize()
+    torch.cuda.empty_cache()
     return int(torch.cuda.mem_get_info()[0])
 
 
@@ -622,30 +600,31 @@ def main():
         e2e = {"value": nviews * args.steps * world / dt, "unit": "projections/s",
                "h2d_bytes_per_step": geometry_bytes, "d2h_bytes_per_step": nviews * W * H * 4}
 
-    # roofline: the texture unit's filtered-fetch rate (binding), and the HBM figures beside it
+    # roofline of the forward kernel: compulsory HBM bytes per launch (one view) over its duration
     peaks = json.loads(PEAKS.read_text()) if PEAKS.exists() else {}
     hbm_peak = peaks.get("hbm_gbs")
     hbm_src = "of measured (MEASURED_PEAKS.json hbm_gbs)"
     if hbm_peak is None:
         hbm_peak, hbm_src = 6800.0, "of fallback (6.8 TB/s)"
-    peak_fetches = texture_rate(args.density_dtype)
     launch_s = ms_per_step / 1000.0 / nviews
     comp = metrics.compulsory_bytes(vols, W, H, args.density_dtype)
     prof = read_profile_figures()
     sha = source_sha()
     stale = prof.get("source_sha") != sha
-    roofline = tex_roofline(samples_per_step / nviews / launch_s, args.density_dtype, peak_fetches)
-    roofline["traffic"] = prof.get("dram_bytes_per_launch")
-    roofline["traffic_note"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch, "
-                                f"profiles/{TRAFFIC_FILE.name}" + (" (captured on an earlier build of the kernels)"
-                                                                    if stale else " (this build)"))
-    roofline["tex_pipe_pct_ncu"] = prof.get("tex_pipe_pct")
-    roofline_hbm = {"bound": "hbm", "achieved": comp / launch_s / 1e9, "peak": hbm_peak, "unit": "GB/s",
-                    "frac": comp / launch_s / 1e9 / hbm_peak, "traffic": prof.get("dram_bytes_per_launch"),
-                    "algorithmic_bytes_per_launch": comp, "l2_hit_pct_ncu": prof.get("l2_hit_pct"),
-                    "l1tex_hit_pct_ncu": prof.get("l1tex_hit_pct"),
-                    "note": "compulsory bytes (each voxel's density + label once, plus the output images) per view, "
-                            f"peak {hbm_src}; not the binding bound: the volume is read from HBM about once per view"}
+    roofline = {"bound": "hbm", "achieved": comp / launch_s / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                "frac": comp / launch_s / 1e9 / hbm_peak, "traffic": prof.get("dram_bytes_per_launch"),
+                "algorithmic_bytes_per_launch": comp,
+                "note": "compulsory bytes (each voxel's density + label once, plus the output images) per view, peak "
+                        f"{hbm_src}; traffic = ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch "
+                        f"(profiles/{TRAFFIC_FILE.name}). The kernel is issue- and texture-bound, see tex_pipe"}
+    sampled_bytes = samples_per_step / nviews * metrics.BYTES_PER_SAMPLE[args.density_dtype]
+    tex_pipe = {"tex_pipe_pct_of_peak_ncu": prof.get("tex_pipe_pct"), "issue_active_pct_ncu": prof.get("issue_active_pct"),
+                "l1tex_hit_pct_ncu": prof.get("l1tex_hit_pct"), "l2_hit_pct_ncu": prof.get("l2_hit_pct"),
+                "ncu_capture_of_this_build": not stale, "kernel_source_sha": sha,
+                "sampled_bytes_per_launch": sampled_bytes, "sampled_gb_per_s": sampled_bytes / launch_s / 1e9,
+                "note": "l1tex__data_pipe_tex_wavefronts and smsp__issue_active as % of peak in the ncu capture of one "
+                        f"launch (profiles/{TRAFFIC_FILE.name}); sampled bytes = 40 B per sample at float32 "
+                        "(8 density + 8 label texels), served by L1/TEX"}
     line = {
         "metric": METRIC, "value": value, "unit": "projections/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -665,8 +644,7 @@ def main():
         "gpu_launches": nviews * args.steps,
         "clocks": clk,
         "roofline": roofline,
-        "roofline_hbm": roofline_hbm,
-        "kernel_source_sha": sha,
+        "tex_pipe": tex_pipe,
         "e2e": e2e,
     }
     if rank == 0 and not args.no_cpu_baseline:
@@ -700,12 +678,8 @@ def main():
         del vols, projs
         line["c1"] = phase_c1(args, local)
         line["batched"] = phase_batched(args, local)
-        line["batched"]["peak_fetches_per_s"] = peak_fetches
-        line["batched"]["roofline"] = tex_roofline(line["batched"]["gsamples_per_s"] * 1e9, "float32", peak_fetches)
         line["adjoint"] = phase_adjoint(args, local)
         line["half"] = phase_half(args, local)
-        line["half"]["roofline_float16"] = tex_roofline(line["half"]["float16"]["gsamples_per_s"] * 1e9, "float16",
-                                                        texture_rate("float16"))
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist is not None:

@@ -1,4 +1,4 @@
-// drr_api.cu -- C ABI of libdrr_gb300.so: volume sets (textures, packed labels), spectrum tables.
+// drr_api.cu -- C ABI of libdrr_gb300.so: volume sets (textures, label codes), spectrum tables.
 //
 // Host-side replacement for deepdrr/projector/projector.py (deepdrr v1.2.2):
 //   create_cuda_texture            projector.py:116-257   -> make_texture()
@@ -96,19 +96,23 @@ void free_volume(Volume &v) {
     if (v.density_tex) cudaDestroyTextureObject(v.density_tex);
     if (v.density_point) cudaDestroyTextureObject(v.density_point);
     if (v.density_array) cudaFreeArray(v.density_array);
-    if (v.packed) cudaFree(v.packed);
     if (v.coded) cudaFree(v.coded);
+    if (v.labels_tex) cudaDestroyTextureObject(v.labels_tex);
+    if (v.labels_array) cudaFreeArray(v.labels_array);
     v = Volume();
 }
 
-// Label words of every base of a volume (see drr::pack_labels_kernel), owned by the volume set.
+// Label codes of every base of a volume (see drr::pack_labels_kernel) and the labels as a uint8
+// texture, owned by the volume set: 2 bytes per base plus 1 byte per voxel.
 drr_status make_label_tables(const uint8_t *src, int ni, int nj, int nk, cudaStream_t s, Volume &v) {
     const size_t np = (size_t)(ni + 1) * (nj + 1) * (nk + 1);
-    DRR_CUDA_TRY(cudaMalloc(&v.packed, np * sizeof(uint32_t)), "cudaMalloc (packed labels)");
-    DRR_CUDA_TRY(cudaMalloc(&v.coded, np * sizeof(uint32_t)), "cudaMalloc (coded labels)");
+    DRR_CUDA_TRY(cudaMalloc(&v.coded, np * sizeof(uint16_t)), "cudaMalloc (label codes)");
+    const drr_status st = make_texture(src, 1, cudaCreateChannelDesc(8, 0, 0, 0, cudaChannelFormatKindUnsigned),
+                                       false, ni, nj, nk, s, &v.labels_array, &v.labels_tex);
+    if (st != DRR_OK) return st;
     const size_t blocks = (np + 255) / 256;
     drr::pack_labels_kernel<<<(unsigned)(blocks < 1048576 ? blocks : 1048576), 256, 0, s>>>(src, ni, nj, nk,
-                                                                                           v.packed, v.coded);
+                                                                                           v.coded);
     DRR_CUDA_TRY(cudaGetLastError(), "pack_labels_kernel launch");
     return DRR_OK;
 }
@@ -116,8 +120,7 @@ drr_status make_label_tables(const uint8_t *src, int ni, int nj, int nk, cudaStr
 }  // namespace
 
 namespace drr {
-__global__ void pack_labels_kernel(const uint8_t *__restrict__ labels, int ni, int nj, int nk, uint32_t *packed,
-                                   uint32_t *coded) {
+__global__ void pack_labels_kernel(const uint8_t *__restrict__ labels, int ni, int nj, int nk, uint16_t *coded) {
     const size_t np = (size_t)(ni + 1) * (nj + 1) * (nk + 1);
     for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < np; e += (size_t)gridDim.x * blockDim.x) {
         const int bi = (int)(e % (ni + 1)) - 1;
@@ -131,9 +134,9 @@ __global__ void pack_labels_kernel(const uint8_t *__restrict__ labels, int ni, i
             const int k = clampi(bk + (c >> 2), 0, nk - 1);
             word |= ((uint32_t)labels[((size_t)k * nj + j) * ni + i] & 15u) << (4 * c);
         }
-        packed[e] = word;
         // A = corner 0's label, B = the first other label (A when there is none), the mask of the
-        // corners labelled B; bit 31 marks a neighbourhood with three or more labels
+        // corners labelled B (bit 0, corner 0's, is always clear); kCodeGeneral marks a neighbourhood
+        // with three or more labels
         const uint32_t A = word & 15u;
         uint32_t B = A, mask = 0u;
         bool general = false;
@@ -147,7 +150,7 @@ __global__ void pack_labels_kernel(const uint8_t *__restrict__ labels, int ni, i
             else
                 general = true;
         }
-        coded[e] = general ? kCodeGeneral : (A | (B << 4) | (mask << 8));
+        coded[e] = (uint16_t)(general ? (kCodeGeneral | A) : (A | (B << 4) | (mask << 8)));
     }
 }
 }  // namespace drr

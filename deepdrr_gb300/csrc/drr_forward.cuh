@@ -20,9 +20,11 @@
 // Differences from the reference, none of which changes a result:
 //   * per-volume state lives in registers (NV, M are template parameters) instead of the
 //     reference's 528-byte local-memory stack frame;
-//   * the eight labels of a 2x2x2 neighbourhood come from one 32-bit load of a precomputed
-//     packed table (4 bits per corner, clamp addressing folded in) instead of eight point-filtered
-//     texture fetches (fetch_label_word explains why this reads exactly the reference's texels);
+//   * the eight labels of a 2x2x2 neighbourhood come from one 16-bit load of a precomputed code
+//     table (the neighbourhood's two labels and which corners hold the second, clamp addressing
+//     folded in) instead of eight point-filtered texture fetches; the rare neighbourhoods with three
+//     or more labels read their eight bytes from a copy of the label volume (fetch_label_word
+//     explains why this reads exactly the reference's texels);
 //   * steps before the first volume interval opens do no sampling (their float32 alpha sequence is
 //     still accumulated step by step, so every later sample position is bit-identical), and the
 //     march stops once alpha has passed the last interval. With more than one volume the last
@@ -59,16 +61,17 @@ constexpr int kMaxSteps = 1 << 26;      // longest march per ray; longer rays ar
 
 struct VolConst {
     cudaTextureObject_t density;  // linear filter, clamp, unnormalised coordinates
-    const uint32_t *packed;       // label words [(nk+1)][(nj+1)][(ni+1)] (pack_labels_kernel), at the entry of
+    const uint16_t *coded;        // label codes [(nk+1)][(nj+1)][(ni+1)] (pack_labels_kernel), at the entry of
                                   // base (0, 0, 0): bases run from -1 to n - 1 on each axis
-    const uint32_t *coded;        // the same neighbourhoods as A | B << 4 | (corners labelled B) << 8, likewise
+    cudaTextureObject_t labels;   // the labels themselves (uint8, point filter, clamp), read for neighbourhoods
+                                  // of three or more labels
     int32_t n[3];                 // ni, nj, nk
     float hi[3];                  // n - 0.5 per axis (projector.py:1626-1634)
     float nm1[3];                 // n - 1 per axis
     int32_t priority;
     int32_t enabled;
-    int32_t row;          // label-table entries per row: n[0] + 1
-    int32_t plane_bytes;  // label-table bytes per plane: 4 (n[0] + 1)(n[1] + 1), below 2^31 because
+    int32_t row;          // code-table entries per row: n[0] + 1
+    int32_t plane_bytes;  // code-table bytes per plane: 2 (n[0] + 1)(n[1] + 1), below 2^31 because
                           // volumes are at most 16384 texels per axis (drr_volset_create)
 };
 
@@ -181,38 +184,77 @@ __device__ __forceinline__ float add_air(float x) {
 __device__ __forceinline__ int clampi(int x, int lo, int hi) { return x < lo ? lo : (x > hi ? hi : x); }
 
 // The eight labels the reference fetches at p + (dx, dy, dz) (point filter: texel clamp(floor)),
-// corner c = dx | dy << 1 | dz << 2 at bits 4c, with (bx, by, bz) = floor(p).
+// with (bx, by, bz) = floor(p) and corner c = dx | dy << 1 | dz << 2.
 // The reference's +1 corners read texel floor(p (+) 1) in float32; that always equals floor(p) + 1
 // here because p = F (-) 1 with F = fma(alpha, r, s) a float: for |p| <= 2, p (+) 1 is exact
 // (Sterbenz), and above that 1 is a multiple of ulp(p) (up to |p| = 2^24, far outside any volume,
-// where both corners clamp to the same texel anyway). So one packed word per base suffices.
-//
-// Entry of base (i, j, k), -1 <= i <= n[0] - 1 etc., of a label table [(n[2]+1)][(n[1]+1)][(n[0]+1)]
+// where both corners clamp to the same texel anyway). So the neighbourhood is a function of the
+// base alone, precomputed per base b in [-1, n-1]^3 (pack_labels_kernel) as a 16-bit code:
+//   bits 0-3   A, corner 0's label
+//   bits 4-7   B, the other label of a two-label neighbourhood (A when there is none)
+//   bits 9-15  the corners 1-7 labelled B (bit 8 + c for corner c)
+//   bit 8      set for a neighbourhood of three or more labels (corner 0 is A by definition, so
+//              this bit is otherwise always clear); its labels are then read from the volume.
+// So a neighbourhood is uniform when code >> 8 == 0.
+constexpr uint32_t kCodeGeneral = 0x100u;
+
+// Entry of base (i, j, k), -1 <= i <= n[0] - 1 etc., of a code table [(n[2]+1)][(n[1]+1)][(n[0]+1)]
 // given at the entry of base (0, 0, 0): the plane by one widening 32 x 32 -> 64-bit multiply, the
 // offset inside it in 32-bit arithmetic (|offset| < (n[0]+1)(n[1]+1) <= 16385^2). This is the address
 // of entry ((k+1)(n[1]+1) + j+1)(n[0]+1) + i+1 of the table's start, computed in 64 bits.
-__device__ __forceinline__ uint32_t label_entry(const uint32_t *origin, const VolConst &V, int i, int j, int k) {
+__device__ __forceinline__ uint32_t label_entry(const uint16_t *origin, const VolConst &V, int i, int j, int k) {
     const char *plane = reinterpret_cast<const char *>(origin) + (long long)k * V.plane_bytes;
-    return __ldg(reinterpret_cast<const uint32_t *>(plane) + (j * V.row + i));
+    return (uint32_t)__ldg(reinterpret_cast<const unsigned short *>(plane) + (j * V.row + i));
 }
 
-__device__ __forceinline__ uint32_t fetch_label_word(const VolConst &V, float bx, float by, float bz) {
-    // packed entry of base clamp(b, -1, n-1) (bases outside behave like the clamped one)
-    const int i = (int)fminf(fmaxf(bx, -1.0f), V.nm1[0]);
-    const int j = (int)fminf(fmaxf(by, -1.0f), V.nm1[1]);
-    const int k = (int)fminf(fmaxf(bz, -1.0f), V.nm1[2]);
-    return label_entry(V.packed, V, i, j, k);
-}
-
-// The same neighbourhood as a code: A (corner 0's label) | B << 4 (the other label, or A) |
-// (mask of the corners labelled B) << 8, or kCodeGeneral for three or more labels (then the word
-// itself is read). Built with the words by pack_labels_kernel.
-constexpr uint32_t kCodeGeneral = 0x80000000u;
+// The code of base clamp(b, -1, n-1) (bases outside behave like the clamped one).
 __device__ __forceinline__ uint32_t fetch_label_code(const VolConst &V, float bx, float by, float bz) {
     const int i = (int)fminf(fmaxf(bx, -1.0f), V.nm1[0]);
     const int j = (int)fminf(fmaxf(by, -1.0f), V.nm1[1]);
     const int k = (int)fminf(fmaxf(bz, -1.0f), V.nm1[2]);
     return label_entry(V.coded, V, i, j, k);
+}
+
+// The packed word of a neighbourhood of three or more labels, 4 bits per corner (corner c at bits
+// 4c..4c+3): the eight texels the reference fetches, read from a uint8 label texture with point
+// filtering and clamp addressing (as projector.py:1500-1519 creates the reference's), at b + d + 0.5,
+// whose texel is clamp(b + d, 0, n - 1). Such neighbourhoods are rare (well under 1 % of a CT's
+// cells): the loop stays rolled so that it needs few registers besides the march's own.
+__device__ __forceinline__ uint32_t gather_label_word(cudaTextureObject_t labels, float bx, float by, float bz) {
+    uint32_t word = 0;
+#pragma unroll 1
+    for (int c = 0; c < 8; c++) {
+        const float x = bx + (float)(c & 1) + 0.5f, y = by + (float)((c >> 1) & 1) + 0.5f, z = bz + (float)(c >> 2) + 0.5f;
+        word |= ((uint32_t)tex3D<unsigned char>(labels, x, y, z) & 15u) << (4 * c);
+    }
+    return word;
+}
+
+// The packed word of a neighbourhood from its code, 4 bits per corner; (bx, by, bz) is the base the
+// code belongs to. Codes of one or two labels expand arithmetically: the mask's bit c moves to bit
+// 4c, and the corners it marks take B instead of A; three or more labels are gathered.
+__device__ __forceinline__ uint32_t code_word(const VolConst &V, uint32_t code, float bx, float by, float bz) {
+    if (code & kCodeGeneral) return gather_label_word(V.labels, bx, by, bz);
+    const uint32_t A = code & 15u, B = (code >> 4) & 15u;
+    uint32_t m = code >> 8;                    // bit c: corner c holds B
+    m = (m | (m << 12)) & 0x000F000Fu;         // spread bit c to bit 4c
+    m = (m | (m << 6)) & 0x03030303u;
+    m = (m | (m << 3)) & 0x11111111u;
+    return (A * 0x11111111u) ^ ((A ^ B) * m);
+}
+
+// The word of base b where its code is known to be kCodeGeneral (b clamped to [-1, n - 1] first,
+// which leaves every corner's clamped texel unchanged).
+__device__ __forceinline__ uint32_t general_label_word(const VolConst &V, float bx, float by, float bz) {
+    return gather_label_word(V.labels, fminf(fmaxf(bx, -1.0f), V.nm1[0]), fminf(fmaxf(by, -1.0f), V.nm1[1]),
+                             fminf(fmaxf(bz, -1.0f), V.nm1[2]));
+}
+
+__device__ __forceinline__ uint32_t fetch_label_word(const VolConst &V, float bx, float by, float bz) {
+    const float cx = fminf(fmaxf(bx, -1.0f), V.nm1[0]);
+    const float cy = fminf(fmaxf(by, -1.0f), V.nm1[1]);
+    const float cz = fminf(fmaxf(bz, -1.0f), V.nm1[2]);
+    return code_word(V, label_entry(V.coded, V, (int)cx, (int)cy, (int)cz), cx, cy, cz);
 }
 
 __device__ __forceinline__ bool uniform_word(uint32_t w) { return w == (w & 15u) * 0x11111111u; }
@@ -494,7 +536,7 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
                     for (int m = 0; m < M; m++)
                         ad[m] = __fmaf_rn(wr, (uint32_t)m == A ? sA : ((uint32_t)m == B ? sB : 0.0f), ad[m]);
                 } else {
-                    word = fetch_label_word(V, cbx, cby, cbz);  // three or more labels: the corners' own
+                    word = general_label_word(V, cbx, cby, cbz);  // three or more labels: the corners' own
                     float seg[M];
                     label_fractions<M>(word, cw, seg);
 #pragma unroll
@@ -591,7 +633,7 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
         float alpha_prev = __int_as_float(0x7fc00000);  // NaN before the first step: the key starts empty
         int key_vol = -1;  // volume whose labels the cached word comes from; the key is (pb0, pb1, pb2)
         uint32_t w_pre[NV];
-        unsigned pre_ok = 0u;  // volumes whose word at this step's base was loaded a step ahead
+        unsigned pre_ok = 0u;  // volumes whose code at this step's base was loaded a step ahead
 #pragma unroll
         for (int i = 0; i < NV; i++) w_pre[i] = 0u;
         int cur_m = -1;  // material whose accumulator is held in cur_ad
@@ -635,28 +677,31 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
                     key_vol = vol;
                 }
                 if (!((adds >> vol) & 1u)) continue;
-                uint32_t w;
-                if (!track || key_vol == vol) {
-                    w = (pre_ok >> vol) & 1u ? w_pre[vol] : fetch_label_word(p.vol[vol], bx, by, bz);
+                // the cached neighbourhood: this volume's own at its base, or the one of the volume
+                // that set the key (the reference's cross-volume cache)
+                uint32_t code;
+                bool own = !track || key_vol == vol;
+                if (own) {
+                    code = (pre_ok >> vol) & 1u ? w_pre[vol] : fetch_label_code(p.vol[vol], bx, by, bz);
                 } else {
-                    w = 0u;
+                    code = 0u;
 #pragma unroll
                     for (int i = 0; i < NV; i++)
-                        if (i == key_vol) w = fetch_label_word(p.vol[i], pb0, pb1, pb2);
+                        if (i == key_vol) code = fetch_label_code(p.vol[i], pb0, pb1, pb2);
                 }
-                {  // this volume's word at the next step's base, loaded now
+                {  // this volume's code at the next step's base, loaded now
                     const float nx = __fsub_rn(__fmaf_rn(an, rxi[vol], s[0]), 1.0f);
                     const float ny = __fsub_rn(__fmaf_rn(an, ryi[vol], s[1]), 1.0f);
                     const float nz = __fsub_rn(__fmaf_rn(an, rzi[vol], s[2]), 1.0f);
-                    w_pre[vol] = fetch_label_word(p.vol[vol], floorf(nx), floorf(ny), floorf(nz));
+                    w_pre[vol] = fetch_label_code(p.vol[vol], floorf(nx), floorf(ny), floorf(nz));
                     pre_next |= 1u << vol;
                 }
                 const CornerWeights cw = corner_weights(__fsub_rn(px, bx), __fsub_rn(py, by), __fsub_rn(pz, bz));
                 const float rho = tex3D<float>(p.vol[vol].density, __fadd_rn(px, 0.5f), __fadd_rn(py, 0.5f),
                                                __fadd_rn(pz, 0.5f));
                 const float wr = __fmul_rn(weight, rho);
-                if (uniform_word(w)) {
-                    const int L = (int)(w & 15u);
+                if ((code >> 8) == 0u) {
+                    const int L = (int)(code & 15u);
                     const float su = uniform_sum(cw);
                     if (L != cur_m) {
                         if (cur_m >= 0) store_ad<M>(ad, cur_m, cur_ad);
@@ -667,10 +712,34 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
                 } else {
                     if (cur_m >= 0) store_ad<M>(ad, cur_m, cur_ad);
                     cur_m = -1;
-                    float seg[M];
-                    label_fractions<M>(w, cw, seg);
+                    if (!(code & kCodeGeneral)) {
+                        // two labels: the same additions as label_fractions makes for their word
+                        const uint32_t A = code & 15u, B = (code >> 4) & 15u, mask = code >> 8;
+                        float sA = 0.0f, sB = 0.0f;
 #pragma unroll
-                    for (int m = 0; m < M; m++) ad[m] = __fmaf_rn(wr, seg[m], ad[m]);
+                        for (int c = 0; c < 8; c++) {
+                            if ((mask >> c) & 1u)
+                                sB = __fmaf_rn(cw.xy[c & 3], cw.z[c >> 2], sB);
+                            else
+                                sA = __fmaf_rn(cw.xy[c & 3], cw.z[c >> 2], sA);
+                        }
+#pragma unroll
+                        for (int m = 0; m < M; m++)
+                            ad[m] = __fmaf_rn(wr, (uint32_t)m == A ? sA : ((uint32_t)m == B ? sB : 0.0f), ad[m]);
+                    } else {
+                        uint32_t w = 0u;
+                        if (own) {
+                            w = general_label_word(p.vol[vol], bx, by, bz);
+                        } else {
+#pragma unroll
+                            for (int i = 0; i < NV; i++)
+                                if (i == key_vol) w = general_label_word(p.vol[i], pb0, pb1, pb2);
+                        }
+                        float seg[M];
+                        label_fractions<M>(w, cw, seg);
+#pragma unroll
+                        for (int m = 0; m < M; m++) ad[m] = __fmaf_rn(wr, seg[m], ad[m]);
+                    }
                 }
             }
             pre_ok = pre_next;
@@ -749,7 +818,7 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
                             ad[m] = __fmaf_rn(wr, (uint32_t)m == A ? sA : ((uint32_t)m == B ? sB : 0.0f), ad[m]);
                     } else {
                         float seg[M];
-                        label_fractions<M>(fetch_label_word(Vv, cbx, cby, cbz), cw, seg);
+                        label_fractions<M>(general_label_word(Vv, cbx, cby, cbz), cw, seg);
 #pragma unroll
                         for (int m = 0; m < M; m++) ad[m] = __fmaf_rn(wr, seg[m], ad[m]);
                     }
@@ -960,10 +1029,9 @@ __global__ void __launch_bounds__(kBlockThreads, forward_min_blocks<NV, M>()) fo
     }
 }
 
-// Packs the labels of every 2x2x2 neighbourhood: word(b) for base b in [-1, n-1]^3 holds the labels
-// at clamp(b + d, 0, n - 1), corner c = dx | dy << 1 | dz << 2 in bits 4c..4c+3.
-__global__ void pack_labels_kernel(const uint8_t *__restrict__ labels, int ni, int nj, int nk, uint32_t *packed,
-                                   uint32_t *coded);
+// Codes the labels of every 2x2x2 neighbourhood: the code of base b in [-1, n-1]^3 describes the labels
+// at clamp(b + d, 0, n - 1), corner c = dx | dy << 1 | dz << 2 (the layout above kCodeGeneral).
+__global__ void pack_labels_kernel(const uint8_t *__restrict__ labels, int ni, int nj, int nk, uint16_t *coded);
 
 // Host-side launcher, explicitly instantiated per (NV, M) in drr_inst_nv*.cu.
 template <int NV, int M>

@@ -298,14 +298,6 @@ drr_status drr_neglog_noalloc(float *images, int32_t n_views, int64_t pixels_per
 /* In-place min(x, upper) over `n` floats: Projector(intensity_upper_bound=...), projector.py:697-698. */
 drr_status drr_clip_upper(float *images, int64_t n, float upper, void *stream);
 
-/* Measurement aid with no counterpart in the reference: the rate, in fetches per second, at which
- * this GPU's texture units return trilinear-filtered samples of an L1-resident 3D texture of
- * `density_type` (DRR_DENSITY_F32 or DRR_DENSITY_F16), timed on `stream` with the forward kernel's
- * launch shape (best of five launches). Every sample of the forward march makes one such fetch, so
- * this is the ceiling of its sample rate. Synchronous; holds a 16^3 texture and a small output
- * buffer for the duration of the call. */
-drr_status drr_texture_rate(int32_t density_type, void *stream, double *fetches_per_second);
-
 /* Human-readable description of the last error raised on this host thread ("" if none). */
 const char *drr_last_error(void);
 

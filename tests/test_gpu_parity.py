@@ -180,6 +180,47 @@ def test_coincident_volumes_share_the_label_cache(nvol):
             assert np.all(d <= 2e-6 * np.abs(ref["area_density"]) + 1e-7), d.max()
 
 
+@pytest.mark.parametrize("nvol", [1, 2])
+def test_three_label_neighbourhoods_match_oracle_and_reference_kernel(nvol):
+    """Random labels over four materials: almost every 2x2x2 neighbourhood holds three or more
+    labels, the case the label-code table only flags, so the kernels read the eight labels from
+    their copy of the label volume. Bit-identical to the full march, within float32 rounding of
+    the oracle, and within 1e-4 of the reference kernel."""
+    rng = np.random.default_rng(41 + nvol)
+    names = ["air", "bone", "soft tissue", "titanium"]
+
+    def random_volume(n, spacing):
+        dens = rng.uniform(0.1, 2.0, (n, n, n)).astype(np.float32)
+        labs = rng.integers(0, 4, (n, n, n))
+        mats = {nm: labs == i for i, nm in enumerate(names)}
+        return dd.Volume.from_parameters(dens, mats, origin=-(n - 1) / 2.0 * spacing * np.ones(3),
+                                         spacing=(spacing,) * 3)
+
+    vols = [random_volume(28, 1.0)]
+    if nvol == 2:
+        b = random_volume(16, 1.3)
+        b.world_from_anatomical = random_rigid(rng, 4.0, 25.0)
+        vols.append(b)
+    names_v, seg = vols[0].materials
+    cells = np.stack([seg[a:a + 27, b:b + 27, c:c + 27] for a in (0, 1) for b in (0, 1) for c in (0, 1)])
+    distinct = sum((cells == i).any(0) for i in range(4))
+    assert (distinct >= 3).mean() > 0.9
+    projs = random_views(2, vols[0].center_in_world, seed=43, sphere_mm=3.0, sensor_size=(20, 18), pixel_size=3.0)
+    got = run_product(vols, projs)
+    full = run_product(vols, projs, flags=_lib.DRR_FLAG_FULL_MARCH)
+    for k in ("intensity", "area_density"):
+        np.testing.assert_array_equal(got[k], full[k])
+    for i, proj in enumerate(projs):
+        sc = oracle_scene(vols, proj)
+        ref = sc.project("f32")
+        assert rel_err(got["intensity"][i], ref["intensity"]).max() <= 2e-6
+        d = np.abs(got["area_density"][i] - ref["area_density"])
+        assert np.all(d <= 2e-6 * np.abs(ref["area_density"]) + 1e-7), d.max()
+        if ref_kernel.available(nvol, 4):
+            rk = ref_kernel.project(sc)
+            assert rel_err(got["intensity"][i], rk["intensity"]).max() <= 1e-4
+
+
 def test_attenuate_outside_matches_oracle():
     vols, projs = small_scene(6)
     got = run_product(vols, projs, attenuate=True)
