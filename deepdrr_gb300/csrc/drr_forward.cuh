@@ -344,10 +344,19 @@ __device__ __forceinline__ float load_ad(const float ad[M], int m_sel) {
     return r;
 }
 
-// The whole computation of one ray: pixel (u, v) of `view`, written to output view `vout`.
+// Shared memory of a block for the per-volume ray state of a multi-volume march: for each thread,
+// kRayState values per volume in its own column [kRayState * NV][kBlockThreads].
+constexpr int kRayState = 5;  // IJK direction x, y, z; entry and exit alpha
+template <int NV>
+constexpr int ray_state_floats() {
+    return NV > 1 ? kRayState * NV * kBlockThreads : 1;
+}
+
+// The whole computation of one ray: pixel (u, v) of `view`, written to output view `vout`. `rs` is
+// this thread's column of the block's ray-state array (unused for one volume).
 template <int NV, int M>
 __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewRec<NV> &view, int u, int v,
-                                           size_t vout) {
+                                           size_t vout, float *rs) {
     const float step = p.step;
     const int nmat = p.n_materials;
 
@@ -404,6 +413,27 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
         minA = fminf(minA, mn);
         maxA = fmaxf(maxA, mx);
     }
+    // The per-volume state the march reads: in registers for one volume; for several, in shared
+    // memory (this thread's column), which keeps the multi-volume march within its 64 registers.
+    unsigned tmask = 0u;  // volumes traced
+#pragma unroll
+    for (int i = 0; i < NV; i++) {
+        if (trace[i]) tmask |= 1u << i;
+        if (NV > 1) {
+            rs[(0 * NV + i) * kBlockThreads] = rxi[i];
+            rs[(1 * NV + i) * kBlockThreads] = ryi[i];
+            rs[(2 * NV + i) * kBlockThreads] = rzi[i];
+            rs[(3 * NV + i) * kBlockThreads] = minv[i];
+            rs[(4 * NV + i) * kBlockThreads] = maxv[i];
+        }
+    }
+    auto RXI = [&](int i) -> float { return NV == 1 ? rxi[0] : rs[(0 * NV + i) * kBlockThreads]; };
+    auto RYI = [&](int i) -> float { return NV == 1 ? ryi[0] : rs[(1 * NV + i) * kBlockThreads]; };
+    auto RZI = [&](int i) -> float { return NV == 1 ? rzi[0] : rs[(2 * NV + i) * kBlockThreads]; };
+    auto MINV = [&](int i) -> float { return NV == 1 ? minv[0] : rs[(3 * NV + i) * kBlockThreads]; };
+    auto MAXV = [&](int i) -> float { return NV == 1 ? maxv[0] : rs[(4 * NV + i) * kBlockThreads]; };
+    auto TRACE = [&](int i) -> bool { return ((tmask >> i) & 1u) != 0u; };
+
     const float span_steps = ceilf(__fdiv_rn(__fsub_rn(maxA, minA), step));
     const size_t plane = (size_t)p.width * (size_t)p.height;
     const size_t pix = (size_t)v * (size_t)p.width + (size_t)u;
@@ -423,9 +453,9 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
     float amin = __int_as_float(0x7f800000), amax = -__int_as_float(0x7f800000);
 #pragma unroll
     for (int i = 0; i < NV; i++) {
-        if (trace[i] && minv[i] <= maxv[i]) {
-            amin = fminf(amin, minv[i]);
-            amax = fmaxf(amax, maxv[i]);
+        if (TRACE(i) && MINV(i) <= MAXV(i)) {
+            amin = fminf(amin, MINV(i));
+            amax = fmaxf(amax, MAXV(i));
         }
     }
 
@@ -474,7 +504,7 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
         // to t = 0 and t = num_steps - 1 only, so those steps are peeled off the main loop.
         const VolConst &V = p.vol[0];
         const float sx = view.vol[0].s[0], sy = view.vol[0].s[1], sz = view.vol[0].s[2];
-        const float rx0 = rxi[0], ry0 = ryi[0], rz0 = rzi[0];
+        const float rx0 = RXI(0), ry0 = RYI(0), rz0 = RZI(0);
         int cur_m = -1;      // material whose accumulator is held in cur_ad
         float cur_ad = 0.0f;
         // Software pipelining of the label words: each step loads the word of the NEXT sample's
@@ -588,13 +618,13 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
             enter = __int_as_float(0x7f800000), leave = __int_as_float(0x7f800000);
 #pragma unroll
             for (int i = 0; i < NV; i++) {
-                if (!trace[i]) continue;
-                if (alpha < minv[i]) {
-                    enter = fminf(enter, minv[i]);
+                if (!TRACE(i)) continue;
+                if (alpha < MINV(i)) {
+                    enter = fminf(enter, MINV(i));
                     continue;
                 }
-                if (alpha > maxv[i]) continue;
-                leave = fminf(leave, maxv[i]);
+                if (alpha > MAXV(i)) continue;
+                leave = fminf(leave, MAXV(i));
                 const int pr = p.vol[i].priority;
                 if (pr < cur) {
                     cur = pr;
@@ -607,7 +637,7 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
             if (n != 0) {
 #pragma unroll
                 for (int i = 0; i < NV; i++)
-                    if (trace[i] && p.vol[i].priority == cur) adds |= 1u << i;
+                    if (TRACE(i) && p.vol[i].priority == cur) adds |= 1u << i;
             }
             wseg = n != 0 ? __fdiv_rn(1.0f, (float)n) : 0.0f;
         };
@@ -622,7 +652,7 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
                 en[i] = p.vol[i].enabled != 0;
                 if (en[i]) last_vol = i;
                 sv[i][0] = view.vol[i].s[0], sv[i][1] = view.vol[i].s[1], sv[i][2] = view.vol[i].s[2];
-                rv[i][0] = rxi[i], rv[i][1] = ryi[i], rv[i][2] = rzi[i];
+                rv[i][0] = RXI(i), rv[i][1] = RYI(i), rv[i][2] = RZI(i);
             }
             double lo, hi;
             coincidence_range(NV, en, sv, rv, step, &lo, &hi);
@@ -655,9 +685,9 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
                 for (int i = 0; i < NV; i++) {
                     if (i != last_vol) continue;
                     const float *s = view.vol[i].s;
-                    pb0 = floorf(__fsub_rn(__fmaf_rn(alpha_prev, rxi[i], s[0]), 1.0f));
-                    pb1 = floorf(__fsub_rn(__fmaf_rn(alpha_prev, ryi[i], s[1]), 1.0f));
-                    pb2 = floorf(__fsub_rn(__fmaf_rn(alpha_prev, rzi[i], s[2]), 1.0f));
+                    pb0 = floorf(__fsub_rn(__fmaf_rn(alpha_prev, RXI(i), s[0]), 1.0f));
+                    pb1 = floorf(__fsub_rn(__fmaf_rn(alpha_prev, RYI(i), s[1]), 1.0f));
+                    pb2 = floorf(__fsub_rn(__fmaf_rn(alpha_prev, RZI(i), s[2]), 1.0f));
                     key_vol = i;
                 }
             }
@@ -668,9 +698,9 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
                 if (!p.vol[vol].enabled) continue;
                 if (!track && !((adds >> vol) & 1u)) continue;
                 const float *s = view.vol[vol].s;
-                const float px = __fsub_rn(__fmaf_rn(alpha, rxi[vol], s[0]), 1.0f);
-                const float py = __fsub_rn(__fmaf_rn(alpha, ryi[vol], s[1]), 1.0f);
-                const float pz = __fsub_rn(__fmaf_rn(alpha, rzi[vol], s[2]), 1.0f);
+                const float px = __fsub_rn(__fmaf_rn(alpha, RXI(vol), s[0]), 1.0f);
+                const float py = __fsub_rn(__fmaf_rn(alpha, RYI(vol), s[1]), 1.0f);
+                const float pz = __fsub_rn(__fmaf_rn(alpha, RZI(vol), s[2]), 1.0f);
                 const float bx = floorf(px), by = floorf(py), bz = floorf(pz);
                 if (track && (bx != pb0 || by != pb1 || bz != pb2)) {
                     pb0 = bx, pb1 = by, pb2 = bz;
@@ -690,9 +720,9 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
                         if (i == key_vol) code = fetch_label_code(p.vol[i], pb0, pb1, pb2);
                 }
                 {  // this volume's code at the next step's base, loaded now
-                    const float nx = __fsub_rn(__fmaf_rn(an, rxi[vol], s[0]), 1.0f);
-                    const float ny = __fsub_rn(__fmaf_rn(an, ryi[vol], s[1]), 1.0f);
-                    const float nz = __fsub_rn(__fmaf_rn(an, rzi[vol], s[2]), 1.0f);
+                    const float nx = __fsub_rn(__fmaf_rn(an, RXI(vol), s[0]), 1.0f);
+                    const float ny = __fsub_rn(__fmaf_rn(an, RYI(vol), s[1]), 1.0f);
+                    const float nz = __fsub_rn(__fmaf_rn(an, RZI(vol), s[2]), 1.0f);
                     w_pre[vol] = fetch_label_code(p.vol[vol], floorf(nx), floorf(ny), floorf(nz));
                     pre_next |= 1u << vol;
                 }
@@ -765,14 +795,11 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
             kk = min(kk, advance_alpha(&a, step, leave, kk, true));       // and not past the end
             if (kk < 2) return false;
             const int v = __ffs(adds) - 1;
-            float vrx = rxi[0], vry = ryi[0], vrz = rzi[0];
+            const float vrx = RXI(v), vry = RYI(v), vrz = RZI(v);
             float vsx = view.vol[0].s[0], vsy = view.vol[0].s[1], vsz = view.vol[0].s[2];
 #pragma unroll
             for (int i = 1; i < NV; i++)
-                if (i == v) {
-                    vrx = rxi[i], vry = ryi[i], vrz = rzi[i];
-                    vsx = view.vol[i].s[0], vsy = view.vol[i].s[1], vsz = view.vol[i].s[2];
-                }
+                if (i == v) vsx = view.vol[i].s[0], vsy = view.vol[i].s[1], vsz = view.vol[i].s[2];
             const VolConst &Vv = p.vol[v];
             // n = 1 and full-weight samples: the weight fl(1 / 1) * rho is rho itself
             float cx = __fsub_rn(__fmaf_rn(alpha, vrx, vsx), 1.0f);
@@ -877,8 +904,8 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
             int cur = NV, n = 0;
 #pragma unroll
             for (int i = 0; i < NV; i++) {
-                if (!trace[i]) continue;
-                if (alpha < minv[i] || alpha > maxv[i]) continue;
+                if (!TRACE(i)) continue;
+                if (alpha < MINV(i) || alpha > MAXV(i)) continue;
                 const int pr = p.vol[i].priority;
                 if (pr < cur) {
                     cur = pr;
@@ -898,9 +925,9 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
             for (int vol = 0; vol < NV; vol++) {
                 if (!p.vol[vol].enabled) continue;
                 const float *s = view.vol[vol].s;
-                const float px = __fsub_rn(__fmaf_rn(alpha, rxi[vol], s[0]), 1.0f);
-                const float py = __fsub_rn(__fmaf_rn(alpha, ryi[vol], s[1]), 1.0f);
-                const float pz = __fsub_rn(__fmaf_rn(alpha, rzi[vol], s[2]), 1.0f);
+                const float px = __fsub_rn(__fmaf_rn(alpha, RXI(vol), s[0]), 1.0f);
+                const float py = __fsub_rn(__fmaf_rn(alpha, RYI(vol), s[1]), 1.0f);
+                const float pz = __fsub_rn(__fmaf_rn(alpha, RZI(vol), s[2]), 1.0f);
                 const float bx = floorf(px), by = floorf(py), bz = floorf(pz);
                 if (bx != pb0 || by != pb1 || bz != pb2) {
                     pb0 = bx;
@@ -910,7 +937,7 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
                     key_ok = false;
                 }
                 // no range re-check, as in project_kernel.cu:541
-                if (n != 0 && !inside && trace[vol] && p.vol[vol].priority == cur) {
+                if (n != 0 && !inside && TRACE(vol) && p.vol[vol].priority == cur) {
                     if (!key_ok) {
 #pragma unroll
                         for (int i = 0; i < NV; i++)
@@ -994,7 +1021,8 @@ __global__ void __launch_bounds__(kBlockThreads, forward_min_blocks<NV, M>()) fo
     const int v = blockIdx.y * kTileH + ((warp >> 1) << 2) + (lane >> 3);
     const int zv = blockIdx.z;
     if (u >= p.s.width || v >= p.s.height || zv >= p.n_views) return;
-    render_ray<NV, M>(p.s, p.views[zv], u, v, (size_t)(p.view0 + zv));
+    __shared__ float rs[ray_state_floats<NV>()];
+    render_ray<NV, M>(p.s, p.views[zv], u, v, (size_t)(p.view0 + zv), rs + threadIdx.x);
 }
 
 // Persistent launch: resident blocks take items_per_grab consecutive (view, tile) items at a time
@@ -1004,6 +1032,7 @@ __global__ void __launch_bounds__(kBlockThreads, forward_min_blocks<NV, M>()) fo
 template <int NV, int M>
 __global__ void __launch_bounds__(kBlockThreads, forward_min_blocks<NV, M>()) forward_persistent_kernel(const __grid_constant__ PersistentParams<NV> p) {
     __shared__ unsigned int s_first;
+    __shared__ float rs[ray_state_floats<NV>()];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const int wx = p.warps_x;
@@ -1024,7 +1053,7 @@ __global__ void __launch_bounds__(kBlockThreads, forward_min_blocks<NV, M>()) fo
             const unsigned int view = it / per_view, tile = it - view * per_view;
             const int u = (int)(tile % (unsigned int)p.tiles_x) * tile_w + du;
             const int v = (int)(tile / (unsigned int)p.tiles_x) * tile_h + dv;
-            if (u < p.s.width && v < p.s.height) render_ray<NV, M>(p.s, p.views[view], u, v, (size_t)view);
+            if (u < p.s.width && v < p.s.height) render_ray<NV, M>(p.s, p.views[view], u, v, (size_t)view, rs + threadIdx.x);
         }
     }
 }
