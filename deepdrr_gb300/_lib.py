@@ -39,7 +39,7 @@ DRR_FLAG_PERSISTENT = 1 << 2
 EXPORTED_SYMBOLS = (
     "drr_volset_create", "drr_volset_destroy", "drr_volset_set_density", "drr_ingest_hu", "drr_tables_create", "drr_tables_destroy",
     "drr_project", "drr_project_adjoint", "drr_graph_create", "drr_graph_set_views", "drr_graph_launch", "drr_graph_destroy",
-    "drr_autotune", "drr_mesh_hits", "drr_mesh_area_density", "drr_add_noise", "drr_poisson_sample", "drr_neglog", "drr_neglog_noalloc", "drr_clip_upper", "drr_last_error", "drr_version",
+    "drr_autotune", "drr_mesh_hits", "drr_mesh_area_density", "drr_add_noise", "drr_poisson_sample", "drr_neglog", "drr_neglog_noalloc", "drr_collected_energy", "drr_clip_upper", "drr_last_error", "drr_version",
 )
 
 
@@ -171,6 +171,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     lib.drr_neglog.restype = st
     lib.drr_neglog_noalloc.argtypes = [vp, i32, ctypes.c_int64, ctypes.c_float, vp]
     lib.drr_neglog_noalloc.restype = st
+    lib.drr_collected_energy.argtypes = [vp, vp, vp, i32, ctypes.c_int64, ctypes.c_double, vp, vp]
+    lib.drr_collected_energy.restype = st
     lib.drr_clip_upper.argtypes = [vp, ctypes.c_int64, ctypes.c_float, vp]
     lib.drr_clip_upper.restype = st
     lib.drr_last_error.argtypes = []

@@ -259,6 +259,82 @@ extern "C" drr_status drr_neglog_noalloc(float *images, int32_t n_views, int64_t
     return DRR_OK;
 }
 
+// ---- drr_collected_energy: Projector(collected_energy=True), projector.py:833-853 ----------------
+//
+// Per view: energy = intensity * solid_angle * photon_count / mean(solid_angle) / pixel_area, in
+// float32 operations in the reference's order (numpy float32 arrays; the mean and the pixel area are
+// scalars rounded to float32). The mean is summed in float64 per view and rounded once, so it is
+// the correctly rounded mean of the view's float32 solid angles.
+namespace {
+
+__global__ void ce_sum(const float *__restrict__ sa, int64_t npix, double *sums) {
+    const int view = blockIdx.y;
+    const float *x = sa + (int64_t)view * npix;
+    double acc = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < npix; i += (int64_t)gridDim.x * blockDim.x)
+        acc += (double)x[i];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(&sums[view], acc);
+}
+
+// The pixel areas of up to kCeViews views, as kernel parameters (no host-to-device copy).
+constexpr int kCeViews = 64;
+struct CeAreas {
+    float area[kCeViews];  // float32(pixel_size_x * pixel_size_y) per view of the launch
+};
+
+__global__ void ce_scale(const float *__restrict__ intensity, const float *__restrict__ sa, float *out, int64_t npix,
+                         const double *sums, const __grid_constant__ CeAreas areas, float photons) {
+    const int view = blockIdx.y;
+    const float mean = (float)(sums[view] / (double)npix);
+    const float area = areas.area[view];
+    const int64_t off = (int64_t)view * npix;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < npix; i += (int64_t)gridDim.x * blockDim.x) {
+        const float e = __fmul_rn(__fmul_rn(intensity[off + i], sa[off + i]), photons);
+        out[off + i] = __fdiv_rn(__fdiv_rn(e, mean), area);
+    }
+}
+
+}  // namespace
+
+extern "C" drr_status drr_collected_energy(const float *intensity, const float *solid_angle, float *out,
+                                           int32_t n_views, int64_t pixels_per_view, double photon_count,
+                                           const double *pixel_area, void *stream) {
+    if (n_views == 0 || pixels_per_view == 0) return DRR_OK;
+    if (!intensity || !solid_angle || !out || !pixel_area || n_views < 0 || pixels_per_view < 0 || n_views > 65535) {
+        drr::set_last_error("drr_collected_energy: bad arguments");
+        return DRR_ERR_INVALID_ARGUMENT;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    double *sums = nullptr;  // per-view float64 sums of the solid angles
+    cudaError_t e = cudaMallocAsync((void **)&sums, sizeof(double) * (size_t)n_views, s);
+    if (e != cudaSuccess) {
+        drr::set_last_error(std::string("drr_collected_energy: cudaMallocAsync: ") + cudaGetErrorString(e));
+        return DRR_ERR_OUT_OF_MEMORY;
+    }
+    e = cudaMemsetAsync(sums, 0, sizeof(double) * (size_t)n_views, s);
+    if (e == cudaSuccess) {
+        ce_sum<<<dim3(blocks_for(pixels_per_view), n_views), kThreads, 0, s>>>(solid_angle, pixels_per_view, sums);
+        e = cudaGetLastError();
+    }
+    for (int v0 = 0; v0 < n_views && e == cudaSuccess; v0 += kCeViews) {
+        const int nv = n_views - v0 < kCeViews ? n_views - v0 : kCeViews;
+        CeAreas a;
+        for (int k = 0; k < kCeViews; k++) a.area[k] = k < nv ? (float)pixel_area[v0 + k] : 1.0f;  // a Python float meets float32
+        const int64_t off = (int64_t)v0 * pixels_per_view;
+        ce_scale<<<dim3(blocks_for(pixels_per_view), nv), kThreads, 0, s>>>(intensity + off, solid_angle + off, out + off,
+                                                                          pixels_per_view, sums + v0, a,
+                                                                          (float)photon_count);
+        e = cudaGetLastError();
+    }
+    cudaFreeAsync(sums, s);
+    if (e != cudaSuccess) {
+        drr::set_last_error(std::string("drr_collected_energy: ") + cudaGetErrorString(e));
+        return DRR_ERR_CUDA;
+    }
+    return DRR_OK;
+}
+
 extern "C" drr_status drr_clip_upper(float *images, int64_t n, float upper, void *stream) {
     if (n == 0) return DRR_OK;
     if (!images || n < 0) {

@@ -602,7 +602,7 @@ class Projector:
         out = self.project_tensors(*camera_projections, stream=stream)
         images = out["intensity"]
         if self.collected_energy:
-            images = self._collected_energy(camera_projections, images, out["solid_angle"]).contiguous()
+            images = self._collected_energy(camera_projections, images, out["solid_angle"], stream)
         lib = _lib.load()
         s = stream if stream is not None else torch.cuda.current_stream(self.torch_device)
         sp = ctypes.c_void_p(s.cuda_stream)
@@ -622,20 +622,21 @@ class Projector:
             _lib.check(lib.drr_neglog(images.data_ptr(), n, h * w, 0.01, sp))
         return images
 
-    def _collected_energy(self, camera_projections, intensity, solid_angle):
-        """projector.py:833-853: intensity * solid angle * photons / mean(solid angle) / pixel area."""
-        projs = self._prepare_project(camera_projections)
-        out = []
-        for i, proj in enumerate(projs):
-            fx = proj.intrinsic.fx
-            fy = proj.intrinsic.fy
-            px = self.source_to_detector_distance / fx
-            py = self.source_to_detector_distance / fy
-            sa = solid_angle[i]
-            e = intensity[i] * sa * self.photon_count / sa.mean()
-            out.append(e / (px * py))
+    def _collected_energy(self, camera_projections, intensity, solid_angle, stream=None):
+        """projector.py:833-853 on the GPU (drr_collected_energy): intensity * solid angle * photons /
+        mean(solid angle) / pixel area, keV per mm^2."""
         import torch
-        return torch.stack(out)
+
+        projs = self._prepare_project(camera_projections)
+        area = np.ascontiguousarray([(self.source_to_detector_distance / proj.intrinsic.fx)
+                                     * (self.source_to_detector_distance / proj.intrinsic.fy) for proj in projs],
+                                    dtype=np.float64)
+        n, h, w = intensity.shape
+        out = torch.empty_like(intensity)
+        _lib.check(_lib.load().drr_collected_energy(intensity.data_ptr(), solid_angle.contiguous().data_ptr(),
+                                                    out.data_ptr(), n, h * w, float(self.photon_count),
+                                                    area.ctypes.data, self._stream_ptr(stream)))
+        return out
 
 
 class ProjectionGraph:

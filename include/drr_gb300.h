@@ -295,6 +295,16 @@ drr_status drr_neglog(float *images, int32_t n_views, int64_t pixels_per_view, f
  * reading them. */
 drr_status drr_neglog_noalloc(float *images, int32_t n_views, int64_t pixels_per_view, float epsilon, void *stream);
 
+/* Collected energy of Projector(collected_energy=True): replaces Projector._calculate_collected_energy_per_pixel
+ * (deepdrr/projector/projector.py:833-853). For `n_views` float32 views of `pixels_per_view` pixels
+ *   out = intensity * solid_angle * photon_count / mean(solid_angle of the view) / pixel_area[view]
+ * (keV per mm^2) in float32 operations in the reference's order; pixel_area (host, [n_views]) is the
+ * reference's (SDD / fx) * (SDD / fy), rounded to float32 as numpy does for a float32 array. The mean
+ * is the correctly rounded float32 mean of the view's solid angles (summed in float64). `out` may be
+ * `intensity`. Uses 8 bytes per view of stream-ordered scratch (cudaMallocAsync). */
+drr_status drr_collected_energy(const float *intensity, const float *solid_angle, float *out, int32_t n_views,
+                                int64_t pixels_per_view, double photon_count, const double *pixel_area, void *stream);
+
 /* In-place min(x, upper) over `n` floats: Projector(intensity_upper_bound=...), projector.py:697-698. */
 drr_status drr_clip_upper(float *images, int64_t n, float upper, void *stream);
 

@@ -259,3 +259,17 @@ def neglog(images: np.ndarray, epsilon: float = 0.01) -> np.ndarray:
     else:
         image = (image - lo) / (hi - lo)
     return image[0] if squeeze else image
+
+
+def collected_energy(intensity: np.ndarray, solid_angle: np.ndarray, photon_count: float, pixel_size_x: float,
+                     pixel_size_y: float) -> np.ndarray:
+    """Collected energy per pixel (keV / mm^2) of one [H, W] view, restating
+    deepdrr/projector/projector.py:833-853 with numpy's float32 semantics: the float32 product of
+    intensity and solid angle, times the photon count, over the float32 mean solid angle (numpy's
+    own float32 mean), over the pixel area (a Python float, applied to the float32 array)."""
+    inten = np.asarray(intensity, dtype=np.float32)
+    sa = np.asarray(solid_angle, dtype=np.float32)
+    mean = np.float32(sa.mean())
+    e = (inten * sa) * np.float32(photon_count)
+    e = e / mean
+    return e / np.float32(pixel_size_x * pixel_size_y)

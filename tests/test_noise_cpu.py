@@ -95,3 +95,58 @@ def test_streams_are_independent_of_order(shim):
     c = np.empty_like(lam)
     shim.poisson_many(lam.ctypes.data, lam.size, 100, c.ctypes.data)
     assert np.mean(a == c) < 0.5
+
+
+# ---- the deterministic part of the noise step, pinned to the reference's own add_noise ----------
+
+GOLDEN_NOISE = HERE / "golden" / "noise_reference.npz"
+
+
+def test_noise_restatement_matches_the_reference_given_the_same_variates():
+    """oracle/noise.py (which the GPU tests hold drr_add_noise to) against the reference's
+    add_noise (analytic_generators.py:10-18) run on the same inputs with np.random.poisson returning
+    the library's variates (tests/golden/make_noise_vectors.py): bit for bit, NaN pattern included."""
+    from oracle.noise import add_noise_given_counts
+
+    g = np.load(GOLDEN_NOISE)
+    got = add_noise_given_counts(g["intensity"], g["photon_prob"], g["counts"], float(g["photon_count"]))
+    np.testing.assert_array_equal(np.isnan(got), np.isnan(g["output"]))
+    assert np.isnan(g["output"]).sum() == 9  # the 3x3 neighbourhood of the photon_prob = 0 pixel
+    np.testing.assert_array_equal(got, g["output"])
+
+
+def test_noise_fixture_holds_the_library_variates(shim):
+    """The fixture's counts are what the library's sampler draws for its lambdas under its seed."""
+    g = np.load(GOLDEN_NOISE)
+    lam = (g["photon_prob"] * np.float32(g["photon_count"])).astype(np.float32).ravel()
+    out = np.empty_like(lam)
+    shim.poisson_many(lam.ctypes.data, lam.size, int(g["seed"]), out.ctypes.data)
+    np.testing.assert_array_equal(out.reshape(g["counts"].shape), g["counts"])
+
+
+def test_noise_fixture_reproduces_with_the_reference_sources():
+    """Where the reference sources are present, its add_noise run again gives the recorded output."""
+    from oracle.build_ref import default_reference
+
+    ref = default_reference()
+    if not (ref / "deepdrr" / "projector" / "analytic_generators.py").is_file():
+        pytest.skip("needs the DeepDRR sources")
+    import sys
+
+    sys.path.insert(0, str(HERE / "golden"))
+    try:
+        import make_noise_vectors as mk
+    finally:
+        sys.path.pop(0)
+    mod = mk.load_reference_module(ref)
+    g = np.load(GOLDEN_NOISE)
+    queue = [g["counts"][i] for i in range(g["counts"].shape[0])]
+    poisson, randn = np.random.poisson, np.random.randn
+    np.random.poisson = lambda lam_i: queue.pop(0).astype(np.int64)
+    np.random.randn = lambda *shape: np.zeros(shape)
+    try:
+        with np.errstate(divide="ignore", invalid="ignore"):
+            out = mod.add_noise(g["intensity"], g["photon_prob"], int(g["photon_count"]))
+    finally:
+        np.random.poisson, np.random.randn = poisson, randn
+    np.testing.assert_array_equal(out, g["output"])
