@@ -64,7 +64,8 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--views", type=int, default=32)
+    ap.add_argument("--views", type=int, default=None,
+                    help="views per step (default: 32 for the headline; each configuration's own count alone)")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--density-dtype", default="float32", choices=["float32", "float16", "bfloat16"])
     ap.add_argument("--workload", default="ct", choices=["ct", "ct512", "multi", "adjoint"],
@@ -342,7 +343,7 @@ def phase_c1(args, local) -> dict:
     return out
 
 
-def phase_batched(args, local) -> dict:
+def phase_batched(args, local, views: int = 256) -> dict:
     """Three volumes, 256 views at 384^2: graph-captured persistent launch vs plain launches, a
     per-view Projector.project loop and the reference kernel."""
     import torch
@@ -350,7 +351,7 @@ def phase_batched(args, local) -> dict:
     import deepdrr_gb300 as dd
     from deepdrr_gb300 import metrics, phantoms, tables
 
-    vols, projs, kw = phantoms.workload_multi(seed=args.seed, views=256)
+    vols, projs, kw = phantoms.workload_multi(seed=args.seed, views=views)
     n = len(projs)
     W, H = projs[0].sensor_width, projs[0].sensor_height
     free0 = free_memory_bytes()
@@ -382,7 +383,7 @@ def phase_batched(args, local) -> dict:
     p.free()
     del graph, p
     torch.cuda.empty_cache()
-    out = {"workload": "multi3_ct512x512x400+256^3+96x96x64_det384_256views_90kV", "views_per_step": n,
+    out = {"workload": f"multi3_ct512x512x400+256^3+96x96x64_det384_{n}views_90kV", "views_per_step": n,
            "graph_projections_per_s": n / (ms_graph / 1000.0), "plain_projections_per_s": n / (ms_plain / 1000.0),
            "speedup_graph_vs_plain": ms_plain / ms_graph, "gsamples_per_s": samples / (ms_graph / 1000.0) / 1e9,
            "autotuned_shape": shape, "resident_bytes": resident, "clocks": clk,
@@ -391,7 +392,7 @@ def phase_batched(args, local) -> dict:
                    "note": "Projector.project(*views) -> host numpy [256, 384, 384] after GPU neglog, against "
                            "[Projector.project(v) for v in views], the reference's serial pattern "
                            "(projector.py:679-685)", "d2h_bytes_per_step": n * W * H * 4},
-           "timing": f"{SUB_WARMUP} warm-up + {SUB_STEPS} timed steps of 256 views"}
+           "timing": f"{SUB_WARMUP} warm-up + {SUB_STEPS} timed steps of {n} views"}
     ref = reference_kernel_times(vols, projs, kw, views=8)
     if "ms_per_view" in ref:
         ref["speedup_graph"] = ref["ms_per_view"] / (ms_graph / n)
@@ -400,7 +401,7 @@ def phase_batched(args, local) -> dict:
     return out
 
 
-def phase_adjoint(args, local) -> dict:
+def phase_adjoint(args, local, views: int = 64) -> dict:
     """2D/3D registration step on the 256^3 phantom, 64 views at 256^2."""
     import numpy as np
     import torch
@@ -409,7 +410,7 @@ def phase_adjoint(args, local) -> dict:
     from deepdrr_gb300 import autograd, tables
     from deepdrr_gb300.phantoms import workload_adjoint
 
-    vols, projs, kw = workload_adjoint(seed=args.seed, views=64)
+    vols, projs, kw = workload_adjoint(seed=args.seed, views=views)
     vol = vols[0]
     n = len(projs)
     W, H = projs[0].sensor_width, projs[0].sensor_height
@@ -461,10 +462,10 @@ def phase_adjoint(args, local) -> dict:
             "memory_bytes": {"stored_peak": mem_stored, "recompute_peak": mem_recompute,
                              "area_density_held": n * M * W * H * 4},
             "pose_grad_cosine_to_target_direction": cos, "clocks": clk,
-            "timing": f"{SUB_WARMUP} warm-up + {SUB_STEPS} timed steps of 64 views"}
+            "timing": f"{SUB_WARMUP} warm-up + {SUB_STEPS} timed steps of {n} views"}
 
 
-def phase_half(args, local) -> dict:
+def phase_half(args, local, views: int = 32) -> dict:
     """512^3 CT, 32 views at 1536^2, 120 kVp: float32 / float16 / bfloat16 density storage."""
     import numpy as np
     import torch
@@ -472,13 +473,13 @@ def phase_half(args, local) -> dict:
     import deepdrr_gb300 as dd
     from deepdrr_gb300 import metrics, phantoms, tables
 
-    vols, projs, kw = phantoms.workload_ct(seed=args.seed, views=32, shape=(512, 512, 512), spectrum="120KV_AL43")
+    vols, projs, kw = phantoms.workload_ct(seed=args.seed, views=views, shape=(512, 512, 512), spectrum="120KV_AL43")
     stream = torch.cuda.current_stream()
     samples = float(metrics.count_samples(vols, projs, kw["step"], -4.0, device=f"cuda:{local}").sum())
     _, _, sample = cpu_baseline(vols, projs, kw, stride=8)
     ids, ref = cpu_baseline.last
     ids_t = torch.from_numpy(ids).to(f"cuda:{local}")
-    out = {"workload": "ct512x512x512_det1536_32views_120kV", "views_per_step": len(projs),
+    out = {"workload": f"ct512x512x512_det1536_{len(projs)}views_120kV", "views_per_step": len(projs),
            "error_sample": sample.replace("extrapolated to whole views", "first view"),
            "timing": f"{SUB_WARMUP} warm-up + {SUB_STEPS} timed steps of 32 views per storage type"}
     for dt in ("float32", "float16", "bfloat16"):
@@ -509,7 +510,7 @@ def run_single(args, rank, world, local):
 
     torch.cuda.set_device(local)
     fn = {"multi": phase_batched, "adjoint": phase_adjoint, "ct512": phase_half}[args.workload]
-    res = fn(args, local)
+    res = fn(args, local) if args.views is None else fn(args, local, views=args.views)
     if rank == 0:
         print(json.dumps({"metric": METRIC, "workload": args.workload, "n_gpus": world, **res}), flush=True)
 
@@ -522,6 +523,8 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
+        if args.views is None:
+            args.views = 32
         return run_reference(args, rank, world)
     if args.workload != "ct" and not args.small:
         return run_single(args, rank, world, local)
@@ -534,6 +537,8 @@ def main():
     from deepdrr_gb300.replicas import max_over_ranks
 
     torch.cuda.set_device(local)
+    if args.views is None:
+        args.views = 32
     dist = None
     if world > 1:
         import torch.distributed as dist

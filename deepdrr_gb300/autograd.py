@@ -60,7 +60,10 @@ def rigid_motion(pose, center) -> np.ndarray:
 
 
 class _State:
-    def __init__(self, projector: Projector, cams, center, recompute: bool, want_area_density: bool):
+    def __init__(self, projector: Projector, cams, center, recompute: bool, want_area_density: bool,
+                 distributed: bool = False, group=None):
+        self.distributed = distributed
+        self.group = group
         self.projector = projector
         self.cams = cams
         self.center = np.asarray(center, dtype=np.float64)
@@ -121,6 +124,16 @@ def _function():
                 density=want_d, pose=want_p, center=c, ijk_from_world=ctx.ijk)
             gd = r["density"].contiguous() if want_d else None
             gp = None
+            if state.distributed:
+                # each rank back-projected its own views: the shared parameters' gradients are sums
+                from .replicas import sum_gradient_
+
+                if gd is not None:
+                    sum_gradient_(gd, state.group)
+                if want_p:
+                    pose_sum = r["pose"].double().sum(0).cpu()
+                    sum_gradient_(pose_sum, state.group)
+                    r["pose"] = pose_sum[None]
             if want_p:
                 g = r["pose"].double().sum(0).cpu().numpy()
                 g[3:] = left_jacobian(ctx.pose_np[3:]).T @ g[3:]
@@ -135,7 +148,7 @@ _PROJECT = None
 
 
 def project(projector: Projector, *camera_projections, density=None, pose=None, center=None,
-            recompute: bool = False, area_density: bool = False) -> dict:
+            recompute: bool = False, area_density: bool = False, distributed: bool = False, group=None) -> dict:
     """Differentiable projection of the projector's single volume.
 
     ``density``: optional CUDA float32 tensor [ni, nj, nk] replacing the volume's densities (its
@@ -144,6 +157,12 @@ def project(projector: Projector, *camera_projections, density=None, pose=None, 
     ``intensity`` and ``photon_prob`` [N, H, W], and with ``area_density`` the per-material area
     densities [N, M, H, W] (g/cm^2, differentiable too). With ``recompute`` the area densities are
     not held from the forward to the backward pass but recomputed there (one more forward pass).
+
+    ``distributed``: the views are this rank's share of a view list sharded over a process group
+    (``group``, default the default group; deepdrr_gb300.replicas.shard gives the shares), each rank
+    holding its own copy of the volume, and the loss is a sum over all ranks' views. The backward
+    then sums the density and pose gradients over the group (one all-reduce of the density
+    gradient, one of the six pose numbers), so every rank gets the gradient of the global loss.
     """
     global _PROJECT
     if len(projector.volumes) != 1:
@@ -154,7 +173,7 @@ def project(projector: Projector, *camera_projections, density=None, pose=None, 
         _PROJECT = _function()
     cams = projector._prepare_project(camera_projections)
     c = projector.volume_center_world(0) if center is None else center
-    state = _State(projector, cams, c, recompute, area_density)
+    state = _State(projector, cams, c, recompute, area_density, distributed, group)
     inten, prob, ad = _PROJECT.apply(density, pose, state)
     out = {"intensity": inten, "photon_prob": prob}
     if area_density:

@@ -38,9 +38,16 @@ def max_over_ranks(value: float, device=None) -> float:
     return float(t.item())
 
 
-def sum_gradient_(grad) -> None:
-    """In-place sum of a gradient tensor over the default process group (no-op without one)."""
+def sum_gradient_(grad, group=None) -> None:
+    """In-place sum of a gradient tensor over `group` (default: the default process group; no-op
+    without one). A gloo group sums through host memory: a CUDA tensor is copied there and back."""
     import torch.distributed as dist
 
-    if dist.is_available() and dist.is_initialized() and dist.get_world_size() > 1:
-        dist.all_reduce(grad, op=dist.ReduceOp.SUM)
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size(group) <= 1:
+        return
+    if grad.is_cuda and dist.get_backend(group) == "gloo":
+        host = grad.detach().cpu()
+        dist.all_reduce(host, op=dist.ReduceOp.SUM, group=group)
+        grad.copy_(host)
+    else:
+        dist.all_reduce(grad, op=dist.ReduceOp.SUM, group=group)
