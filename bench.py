@@ -192,11 +192,11 @@ def read_profile_figures() -> dict:
             if ln.startswith("#") or ":" not in ln:
                 continue
             key, _, val = ln.partition(":")
-            val = val.strip()
+            key, val = key.strip(), val.strip()
             try:
-                out[key.strip()] = float(val)
+                out[key] = val if key == "source_sha" else float(val)
             except ValueError:
-                out[key.strip()] = val
+                out[key] = val
     return out
 
 
