@@ -180,7 +180,7 @@ struct AdjointWarpSmem {
     uint32_t mix[kMixWords][kAdjQueue];  // runs in cells with mixed labels, set aside by the drain
     float gr[M][32];   // each lane's material weights gr_m
     float ray[9][32];  // each lane's unit ray in IJK (0-2), source in IJK (3-5), unit ray in world (6-8)
-    float pose[6][32];  // each lane's share of the drained pose sums: h (IJK, 0-2), r x A^T hk (3-5)
+    float pose[6][32];  // each lane's share of the drained h sums (IJK, 0-2); each ray's hk sum (IJK, 3-5)
     float A[9];        // the view's IJK_from_world rotation
 };
 
@@ -196,14 +196,18 @@ __device__ __forceinline__ void red_add_pair(float *a, float x, float y) {
 // Adds v[c] to texel c = dx | dy << 1 | dz << 2 of the filter cell with lower corner (i0, j0, k0):
 // texel (min(i0 + dx, n0 - 1), ...) of the [n2][n1][n0] gradient volume, as the texture's clamp
 // addressing reads it. The two texels of a row are adjacent and go out as one vector reduction.
+// Volumes of at most 32767 texels per axis (drr_project_adjoint's limit) keep a plane's offsets below
+// 2^31, so the rows are addressed as a plane pointer (one widening multiply) plus 32-bit offsets.
 __device__ __forceinline__ void scatter_cell(float *grad, int i0, int j0, int k0, int n0, int n1, int n2,
                                              const float v[8]) {
     const int j1 = min(j0 + 1, n1 - 1), k1 = min(k0 + 1, n2 - 1);
+    const int plane = n0 * n1;
+    float *const p0 = grad + (long long)k0 * plane, *const p1 = grad + (long long)k1 * plane;
+    const int o0 = j0 * n0 + i0, o1 = j1 * n0 + i0;
 #pragma unroll
     for (int row = 0; row < 4; row++) {
-        const int j = row & 1 ? j1 : j0, k = row & 2 ? k1 : k0;
         const float x = v[2 * row], y = v[2 * row + 1];
-        float *a = grad + ((size_t)k * n1 + j) * n0 + i0;
+        float *a = (row & 2 ? p1 : p0) + (row & 1 ? o1 : o0);
         if (i0 + 1 >= n0) {  // clamped edge: both corners are the same texel
             if (x + y != 0.0f) atomicAdd(a, x + y);
         } else if (x != 0.0f || y != 0.0f) {
@@ -222,18 +226,17 @@ __device__ __forceinline__ int hw_fix_live(float p) {
     return max(__float2int_rd(__fmaf_rn(__fadd_rn(p, 0.5f), 256.0f, -127.5f)), 0);
 }
 
-// The IJK sum h and r_owner x (A^T hk) in world coordinates, into lane `lane`'s pose sums.
+// Pose sums of one run or sample: the IJK sum h into lane `lane`'s share, and the alpha-weighted sum
+// hk into the owner ray's own sum. The moment r x (A^T hk) is linear in hk and r is the owner's, so
+// it is taken once per ray at the end instead of once per run; lanes of one warp may add to the same
+// owner in one drain, hence the shared-memory atomics.
 template <int M>
 __device__ __forceinline__ void add_pose_sums(AdjointWarpSmem<M> &sh, int lane, const float h[3], const float hk[3],
                                               int owner) {
     sh.pose[0][lane] += h[0], sh.pose[1][lane] += h[1], sh.pose[2][lane] += h[2];
-    const float kx = sh.A[0] * hk[0] + sh.A[3] * hk[1] + sh.A[6] * hk[2];
-    const float ky = sh.A[1] * hk[0] + sh.A[4] * hk[1] + sh.A[7] * hk[2];
-    const float kz = sh.A[2] * hk[0] + sh.A[5] * hk[1] + sh.A[8] * hk[2];
-    const float ox = sh.ray[6][owner], oy = sh.ray[7][owner], oz = sh.ray[8][owner];
-    sh.pose[3][lane] += oy * kz - oz * ky;
-    sh.pose[4][lane] += oz * kx - ox * kz;
-    sh.pose[5][lane] += ox * ky - oy * kx;
+    atomicAdd(&sh.pose[3][owner], hk[0]);
+    atomicAdd(&sh.pose[4][owner], hk[1]);
+    atomicAdd(&sh.pose[5][owner], hk[2]);
 }
 
 // One sample of a mixed-label cell at float32 alpha `al` of ray `owner` (label word `word`): the
@@ -416,10 +419,14 @@ __global__ void __launch_bounds__(kBlockThreads, M <= 4 ? 6 : 5) adjoint_kernel(
             const float py = __fsub_rn(__fmaf_rn(al, ryi, sh.ray[4][owner]), 1.0f);
             const float pz = __fsub_rn(__fmaf_rn(al, rzi, sh.ray[5][owner]), 1.0f);
             const float bx = floorf(px), by = floorf(py), bz = floorf(pz);
-            word = fetch_label_word(V, bx, by, bz);
-            mixed = !uniform_word(word);
+            // the cell's label code; the packed word only for a run in a mixed cell
+            const float cbx = fminf(fmaxf(bx, -1.0f), V.nm1[0]), cby = fminf(fmaxf(by, -1.0f), V.nm1[1]);
+            const float cbz = fminf(fmaxf(bz, -1.0f), V.nm1[2]);
+            const uint32_t code = label_entry(V.coded, V, (int)cbx, (int)cby, (int)cbz);
+            mixed = (code >> 8) != 0u;
+            if (mixed) word = code_word(V, code, cbx, cby, cbz);
             if (!mixed) {
-                const float gu = sh.gr[word & 15u][owner];
+                const float gu = sh.gr[code & 15u][owner];
                 if (do_dens) {
                     // every sample adds w_t gu W_c / 256 to texel c: the packed sums hold sum W_c
                     const float rv = __fmul_rn(__fmul_rn(wrun, gu), 1.0f / 256.0f);
@@ -609,9 +616,20 @@ __global__ void __launch_bounds__(kBlockThreads, M <= 4 ? 6 : 5) adjoint_kernel(
     drain_mixed<M>(P, sh, lane, mhead, mqueued);
 
     if (do_pose) {
-        // the warp's pose sums: one atomic per component
+        // the warp's pose sums: each ray's moment r x (A^T hk), then one atomic per component
+        __syncwarp();
         float Hs0 = sh.pose[0][lane], Hs1 = sh.pose[1][lane], Hs2 = sh.pose[2][lane];
-        float Cs0 = sh.pose[3][lane], Cs1 = sh.pose[4][lane], Cs2 = sh.pose[5][lane];
+        float Cs0, Cs1, Cs2;
+        {
+            const float h0 = sh.pose[3][lane], h1 = sh.pose[4][lane], h2 = sh.pose[5][lane];
+            const float kx = sh.A[0] * h0 + sh.A[3] * h1 + sh.A[6] * h2;
+            const float ky = sh.A[1] * h0 + sh.A[4] * h1 + sh.A[7] * h2;
+            const float kz = sh.A[2] * h0 + sh.A[5] * h1 + sh.A[8] * h2;
+            const float ox = sh.ray[6][lane], oy = sh.ray[7][lane], oz = sh.ray[8][lane];
+            Cs0 = oy * kz - oz * ky;
+            Cs1 = oz * kx - ox * kz;
+            Cs2 = ox * ky - oy * kx;
+        }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             Hs0 += __shfl_xor_sync(kAll, Hs0, o);
