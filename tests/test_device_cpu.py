@@ -2,6 +2,7 @@
 SimpleDevice / MobileCArm definitions imply (deepdrr/device/simple_device.py,
 mobile_carm.py), checked on the camera projections they produce."""
 import math
+from pathlib import Path
 
 import numpy as np
 import pytest
@@ -143,3 +144,41 @@ def test_projector_takes_its_view_from_a_device():
     np.testing.assert_allclose(s, s2)
     assert (w, h) == (48, 32)
     assert abs(p.max_ray_length - math.sqrt(1020.0 ** 2 + (32 * 4.0) ** 2 + (48 * 4.0) ** 2)) < 1e-9
+
+
+# ---- pinned to the reference's own device classes -------------------------------------------------
+
+DEVICE_GOLDEN = Path(__file__).resolve().parent / "golden" / "device_reference.npz"
+
+
+def _replay(sc):
+    from deepdrr_gb300.device import MobileCArm, SimpleDevice
+    from deepdrr_gb300.geo import FrameTransform
+
+    init = dict(sc["init"])
+    if "world_from_device" in init:
+        init["world_from_device"] = FrameTransform(np.array(init["world_from_device"]))
+    d = SimpleDevice(**init) if sc["kind"] == "simple" else MobileCArm(**init)
+    for name, kw in sc["ops"]:
+        getattr(d, name)(**kw)
+    return d
+
+
+def test_devices_reproduce_the_reference_device_classes():
+    """camera3d_from_world, intrinsics and C-arm state of this package's SimpleDevice / MobileCArm
+    against the reference's own classes (deepdrr/device/simple_device.py, mobile_carm.py) run on the
+    same seeded scenarios by tests/golden/make_device_vectors.py (killeengeo replaced by
+    tests/golden/geo_standin.py): equal to 1e-9."""
+    import json
+
+    g = np.load(DEVICE_GOLDEN)
+    scs = json.loads(str(g["scenarios"]))
+    assert len(scs) >= 20
+    for i, sc in enumerate(scs):
+        d = _replay(sc)
+        np.testing.assert_allclose(np.asarray(d.camera3d_from_world.data), g[f"s{i}__camera3d_from_world"],
+                                   rtol=0, atol=1e-9, err_msg=f"scenario {i} ({sc['kind']})")
+        np.testing.assert_allclose(np.asarray(d.camera_intrinsics.data), g[f"s{i}__intrinsic"], rtol=1e-15, atol=0)
+        if sc["kind"] == "carm":
+            np.testing.assert_allclose(d.isocenter, g[f"s{i}__isocenter"], rtol=0, atol=1e-9)
+            np.testing.assert_allclose([d.alpha, d.beta, d.gamma], g[f"s{i}__angles"], rtol=0, atol=1e-12)
