@@ -380,6 +380,7 @@ def phase_batched(args, local, views: int = 256) -> dict:
 
     e2e_batched = wall(lambda: p.project(*projs))
     e2e_loop = wall(lambda: [p.project(pr) for pr in projs])
+    small = small_views_regime(p, vols, kw, local) if views >= 64 else None
     p.free()
     del graph, p
     torch.cuda.empty_cache()
@@ -398,7 +399,33 @@ def phase_batched(args, local, views: int = 256) -> dict:
         ref["speedup_graph"] = ref["ms_per_view"] / (ms_graph / n)
         ref["speedup_plain"] = ref["ms_per_view"] / (ms_plain / n)
     out["reference_kernel"] = ref
+    if small is not None:
+        out["small_views"] = small
     return out
+
+
+def small_views_regime(p, vols, kw, local, n: int = 2048, side: int = 32, seed: int = 17) -> dict:
+    """The same three volumes seen by `n` views of side^2 pixels covering the 384^2 views' field:
+    one view is too few rays to fill the GPU, so a plain launch per view is bound by the latency of
+    its rays, and the persistent launch, which keeps every view's rays in flight together, is not."""
+    import torch
+
+    from deepdrr_gb300 import phantoms
+
+    projs = phantoms.random_views(n, vols[0].center_in_world, seed=seed, sphere_mm=100.0, cone_deg=30.0,
+                                  source_to_detector_distance=1020.0, pixel_size=0.3 * 384 / side,
+                                  sensor_size=(side, side), fraction_range=(0.5, 0.9))
+    stream = torch.cuda.current_stream()
+    shape = p.autotune(*projs, max_views=256, cache=False)
+    graph = p.capture(*projs, launch=shape)
+    ms_graph = timed_events(lambda: graph.launch(), SUB_WARMUP, SUB_STEPS, stream)
+    graph.close()
+    ms_plain = timed_events(lambda: [p.project_tensors(pr) for pr in projs], 1, 1, stream)
+    return {"workload": f"multi3_det{side}_{n}views_90kV", "views_per_step": n,
+            "graph_projections_per_s": n / (ms_graph / 1000.0), "plain_projections_per_s": n / (ms_plain / 1000.0),
+            "speedup_graph_vs_plain": ms_plain / ms_graph, "autotuned_shape": shape,
+            "timing": f"graph: {SUB_WARMUP} warm-up + {SUB_STEPS} timed steps; plain: 1 + 1 steps of {n} launches"}
+
 
 
 def phase_adjoint(args, local, views: int = 64) -> dict:
