@@ -567,47 +567,44 @@ __global__ void __launch_bounds__(kBlockThreads, M <= 4 ? 6 : 5) adjoint_kernel(
         alpha = __fadd_rn(alpha, step);
         ++t;
     }
-    bool live = t < t_stop;
-    float cx = 0.0f, cy = 0.0f, cz = 0.0f;
-    if (live) {
-        cx = __fsub_rn(__fmaf_rn(alpha, R.rxi, R.sx), 1.0f);
-        cy = __fsub_rn(__fmaf_rn(alpha, R.ryi, R.sy), 1.0f);
-        cz = __fsub_rn(__fmaf_rn(alpha, R.rzi, R.sz), 1.0f);
-    }
-    while (__any_sync(kAll, live || K > 0)) {
-        bool fresh = false;
+    // The warp runs its longest ray's full-weight samples plus one step that closes the last runs,
+    // a bound known up front (one reduction), so the loop needs no vote per step. A lane past its
+    // own samples computes positions it does not use; its run state changes only through selects.
+    const int my_steps = t < t_stop ? t_stop - t : 0;
+    const int warp_steps = __reduce_max_sync(kAll, my_steps) + 1;
+    float cx = __fsub_rn(__fmaf_rn(alpha, R.rxi, R.sx), 1.0f);
+    float cy = __fsub_rn(__fmaf_rn(alpha, R.ryi, R.sy), 1.0f);
+    float cz = __fsub_rn(__fmaf_rn(alpha, R.rzi, R.sz), 1.0f);
+#pragma unroll 2
+    for (int it = 0; it < warp_steps; ++it) {
+        const bool live = it < my_steps;
+        const float bx = floorf(cx), by = floorf(cy), bz = floorf(cz);
         int fxi = 0, fyi = 0, fzi = 0;
-        float bx = 0.0f, by = 0.0f, bz = 0.0f;
-        if (live) {
-            bx = floorf(cx), by = floorf(cy), bz = floorf(cz);
-            fresh = K == 0 || K == 255 || bx != rbx || by != rby || bz != rbz;
-            if (do_dens) {
-                fxi = hw_fix_live(cx), fyi = hw_fix_live(cy), fzi = hw_fix_live(cz);
-                fresh = fresh || ((fxi ^ rfx) | (fyi ^ rfy) | (fzi ^ rfz)) >= 256;
-            }
+        bool fresh = K == 0 || K == 255 || bx != rbx || by != rby || bz != rbz;
+        if (do_dens) {
+            fxi = hw_fix_live(cx), fyi = hw_fix_live(cy), fzi = hw_fix_live(cz);
+            fresh = fresh || ((fxi ^ rfx) | (fyi ^ rfy) | (fzi ^ rfz)) >= 256;
         }
         // a run ends when this sample starts a new one or the ray has no full-weight samples left
         enqueue(K > 0 && (!live || fresh), false);
-        if (live) {
-            if (K == 0) {
-                a0 = alpha;
-                rbx = bx, rby = by, rbz = bz;
-                rfx = fxi, rfy = fyi, rfz = fzi;
-                S0 = S1 = S2 = S3 = 0u;
-            }
-            if (do_dens) {
-                uint32_t Wp[4];
-                packed_corner_weights((uint32_t)fxi & 255u, (uint32_t)fyi & 255u, (uint32_t)fzi & 255u, Wp);
-                S0 += Wp[0], S1 += Wp[1], S2 += Wp[2], S3 += Wp[3];
-            }
-            ++K;
-            ++t;
-            alpha = __fadd_rn(alpha, step);
-            cx = __fsub_rn(__fmaf_rn(alpha, R.rxi, R.sx), 1.0f);
-            cy = __fsub_rn(__fmaf_rn(alpha, R.ryi, R.sy), 1.0f);
-            cz = __fsub_rn(__fmaf_rn(alpha, R.rzi, R.sz), 1.0f);
-            live = t < t_stop;
+        const bool open = live && K == 0;  // this sample starts a run
+        a0 = open ? alpha : a0;
+        rbx = open ? bx : rbx, rby = open ? by : rby, rbz = open ? bz : rbz;
+        rfx = open ? fxi : rfx, rfy = open ? fyi : rfy, rfz = open ? fzi : rfz;
+        if (do_dens) {
+            uint32_t Wp[4];
+            packed_corner_weights((uint32_t)fxi & 255u, (uint32_t)fyi & 255u, (uint32_t)fzi & 255u, Wp);
+            S0 = (open ? 0u : S0) + (live ? Wp[0] : 0u);
+            S1 = (open ? 0u : S1) + (live ? Wp[1] : 0u);
+            S2 = (open ? 0u : S2) + (live ? Wp[2] : 0u);
+            S3 = (open ? 0u : S3) + (live ? Wp[3] : 0u);
         }
+        K += live ? 1 : 0;
+        t += live ? 1 : 0;
+        alpha = live ? __fadd_rn(alpha, step) : alpha;
+        cx = __fsub_rn(__fmaf_rn(alpha, R.rxi, R.sx), 1.0f);
+        cy = __fsub_rn(__fmaf_rn(alpha, R.ryi, R.sy), 1.0f);
+        cz = __fsub_rn(__fmaf_rn(alpha, R.rzi, R.sz), 1.0f);
     }
     single(last_half);
     __syncwarp();
