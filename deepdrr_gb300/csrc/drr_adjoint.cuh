@@ -223,7 +223,9 @@ __device__ __forceinline__ int hw_fix(float p, int n) {
     return hw_fix_from_floor(__float2int_rd(__fmaf_rn(__fadd_rn(p, 0.5f), 256.0f, -127.5f)), n);
 }
 __device__ __forceinline__ int hw_fix_live(float p) {
-    return max(__float2int_rd(__fmaf_rn(__fadd_rn(p, 0.5f), 256.0f, -127.5f)), 0);
+    // the conversion to unsigned saturates: a negative value (a coordinate below the first texel
+    // centre) becomes 0, the texture's lower clamp
+    return (int)__float2uint_rd(__fmaf_rn(__fadd_rn(p, 0.5f), 256.0f, -127.5f));
 }
 
 // Pose sums of one run or sample: the IJK sum h into lane `lane`'s share, and the alpha-weighted sum
@@ -594,10 +596,11 @@ __global__ void __launch_bounds__(kBlockThreads, M <= 4 ? 6 : 5) adjoint_kernel(
         if (do_dens) {
             uint32_t Wp[4];
             packed_corner_weights((uint32_t)fxi & 255u, (uint32_t)fyi & 255u, (uint32_t)fzi & 255u, Wp);
-            S0 = (open ? 0u : S0) + (live ? Wp[0] : 0u);
-            S1 = (open ? 0u : S1) + (live ? Wp[1] : 0u);
-            S2 = (open ? 0u : S2) + (live ? Wp[2] : 0u);
-            S3 = (open ? 0u : S3) + (live ? Wp[3] : 0u);
+            // a lane past its samples adds to sums that are never queued again (its run is closed)
+            S0 = (open ? 0u : S0) + Wp[0];
+            S1 = (open ? 0u : S1) + Wp[1];
+            S2 = (open ? 0u : S2) + Wp[2];
+            S3 = (open ? 0u : S3) + Wp[3];
         }
         K += live ? 1 : 0;
         t += live ? 1 : 0;
