@@ -196,6 +196,24 @@ __device__ __forceinline__ void red_add_pair(float *a, float x, float y) {
 // Adds v[c] to texel c = dx | dy << 1 | dz << 2 of the filter cell with lower corner (i0, j0, k0):
 // texel (min(i0 + dx, n0 - 1), ...) of the [n2][n1][n0] gradient volume, as the texture's clamp
 // addressing reads it. The two texels of a row are adjacent and go out as one vector reduction.
+// rv * W for the eight corner weights packed two to a word (P[dx * 2 + dy] = W(dz = 0) | W(dz = 1) << 16,
+// drr_texweights.h), ordered for scatter_cell (v[2 row + dx] with row = dy | dz << 1). A 16-bit count
+// becomes a float through the exponent field (2^23 + count is exact below 2^23), and one fused
+// multiply-add gives rv * count rounded once, as rv * (float)count would: no integer-to-float
+// conversions.
+__device__ __forceinline__ void weighted_corners(const uint32_t P[4], float rv, float v[8]) {
+    const float bias = __fmul_rn(rv, 8388608.0f);  // rv * 2^23, exact
+#pragma unroll
+    for (int row = 0; row < 4; row++) {
+        const int dy = row & 1, dz = row >> 1;
+#pragma unroll
+        for (int dx = 0; dx < 2; dx++) {
+            const uint32_t cnt = (P[dx * 2 + dy] >> (16 * dz)) & 0xFFFFu;
+            v[2 * row + dx] = __fmaf_rn(rv, __uint_as_float(0x4B000000u | cnt), -bias);
+        }
+    }
+}
+
 // Volumes of at most 32767 texels per axis (drr_project_adjoint's limit) keep a plane's offsets below
 // 2^31, so the rows are addressed as a plane pointer (one widening multiply) plus 32-bit offsets.
 __device__ __forceinline__ void scatter_cell(float *grad, int i0, int j0, int k0, int n0, int n1, int n2,
@@ -265,14 +283,10 @@ __device__ __forceinline__ void mixed_sample(const AdjointParams &P, AdjointWarp
         const int fxi = hw_fix(px, n0), fyi = hw_fix(py, n1), fzi = hw_fix(pz, n2);
         uint32_t Wp[4];
         packed_corner_weights((uint32_t)fxi & 255u, (uint32_t)fyi & 255u, (uint32_t)fzi & 255u, Wp);
-        const int i0 = fxi >> 8, j0 = fyi >> 8, k0 = fzi >> 8;
-        const int i1 = min(i0 + 1, n0 - 1), j1 = min(j0 + 1, n1 - 1), k1 = min(k0 + 1, n2 - 1);
-#pragma unroll 1
-        for (int c = 0; c < 8; c++) {
-            const int dx = c & 1, dy = (c >> 1) & 1, dz = c >> 2;
-            const float w = (float)((Wp[dx * 2 + dy] >> (16 * dz)) & 0xFFFFu);
-            if (w != 0.0f && rv != 0.0f)
-                atomicAdd(P.grad_density + ((size_t)(dz ? k1 : k0) * n1 + (dy ? j1 : j0)) * n0 + (dx ? i1 : i0), rv * w);
+        if (rv != 0.0f) {
+            float vals[8];
+            weighted_corners(Wp, rv, vals);
+            scatter_cell(P.grad_density, fxi >> 8, fyi >> 8, fzi >> 8, n0, n1, n2, vals);
         }
     }
     if (P.grad_pose != nullptr) {
@@ -432,15 +446,9 @@ __global__ void __launch_bounds__(kBlockThreads, M <= 4 ? 6 : 5) adjoint_kernel(
                 if (do_dens) {
                     // every sample adds w_t gu W_c / 256 to texel c: the packed sums hold sum W_c
                     const float rv = __fmul_rn(__fmul_rn(wrun, gu), 1.0f / 256.0f);
+                    const uint32_t sums[4] = {sh.run[2][e], sh.run[3][e], sh.run[4][e], sh.run[5][e]};
                     float vals[8];
-#pragma unroll
-                    for (int row = 0; row < 4; row++) {
-                        // packed word of (dx, dy) holds dz = 0 | dz = 1 << 16
-                        const int dy = row & 1, dz = row >> 1;
-                        const uint32_t s0 = sh.run[2 + dy][e], s1 = sh.run[4 + dy][e];
-                        vals[2 * row] = rv * (float)((s0 >> (16 * dz)) & 0xFFFFu);
-                        vals[2 * row + 1] = rv * (float)((s1 >> (16 * dz)) & 0xFFFFu);
-                    }
+                    weighted_corners(sums, rv, vals);
                     scatter_cell(grad, hw_fix(px, n0) >> 8, hw_fix(py, n1) >> 8, hw_fix(pz, n2) >> 8, n0, n1, n2,
                                  vals);
                 }
