@@ -176,6 +176,32 @@ __device__ __forceinline__ float pixel_solid_angle(const float *w, int udx, int 
     return sa012 + sa023;
 }
 
+// Paired float32 arithmetic: sm_103a's f32x2 instructions apply the scalar operation to two
+// independent lanes in one instruction, each lane rounded to nearest exactly as __fmaf_rn /
+// __fadd_rn / __fsub_rn / __fmul_rn round it (no flush of subnormals), so pairing the x and y halves
+// of the march's vector arithmetic changes no result and saves an instruction per pair.
+__device__ __forceinline__ float2 fma2_rn(float2 a, float2 b, float2 c) {
+    float2 r;
+    asm("{\n\t.reg .b64 ra, rb, rc, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\tmov.b64 rc, {%6, %7};"
+        "\n\tfma.rn.f32x2 rd, ra, rb, rc;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+        : "=f"(r.x), "=f"(r.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+    return r;
+}
+__device__ __forceinline__ float2 add2_rn(float2 a, float2 b) {
+    float2 r;
+    asm("{\n\t.reg .b64 ra, rb, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\tadd.rn.f32x2 rd, ra, rb;"
+        "\n\tmov.b64 {%0, %1}, rd;\n\t}"
+        : "=f"(r.x), "=f"(r.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return r;
+}
+__device__ __forceinline__ float2 sub2_rn(float2 a, float2 b) {
+    float2 r;
+    asm("{\n\t.reg .b64 ra, rb, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\tsub.rn.f32x2 rd, ra, rb;"
+        "\n\tmov.b64 {%0, %1}, rd;\n\t}"
+        : "=f"(r.x), "=f"(r.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return r;
+}
+
 __device__ __forceinline__ float add_air(float x) {
     // area_density[AIR_INDEX] += AIR_DENSITY: a float32 accumulator plus a double literal
     return (float)((double)x + kAirDensity);
@@ -503,40 +529,53 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
         // ever holds this volume's labels. The trapezoid half weights (project_kernel.cu:537) apply
         // to t = 0 and t = num_steps - 1 only, so those steps are peeled off the main loop.
         const VolConst &V = p.vol[0];
-        const float sx = view.vol[0].s[0], sy = view.vol[0].s[1], sz = view.vol[0].s[2];
-        const float rx0 = RXI(0), ry0 = RYI(0), rz0 = RZI(0);
+        // x and y travel as pairs (f32x2 arithmetic, the same roundings as the scalar operations)
+        const float2 s2 = make_float2(view.vol[0].s[0], view.vol[0].s[1]);
+        const float sz = view.vol[0].s[2];
+        const float2 r2 = make_float2(RXI(0), RYI(0));
+        const float rz0 = RZI(0);
+        const float2 one2 = make_float2(1.0f, 1.0f), half2v = make_float2(0.5f, 0.5f);
+        const float2 step2 = make_float2(step, step);
+        float2 a2 = make_float2(alpha, alpha);  // alpha in both lanes
         int cur_m = -1;      // material whose accumulator is held in cur_ad
         float cur_ad = 0.0f;
         // Software pipelining of the label words: each step loads the word of the NEXT sample's
         // base, so the load's latency overlaps this sample's work and no lane branches to fetch.
         // With one volume the reference's cache always holds the current base's word, so loading
         // it for every sample is the same thing.
-        float cx = 0.0f, cy = 0.0f, cz = 0.0f, cbx = 0.0f, cby = 0.0f, cbz = 0.0f;
+        float2 c2 = make_float2(0.0f, 0.0f), cb2 = make_float2(0.0f, 0.0f);
+        float cz = 0.0f, cbz = 0.0f;
         uint32_t w_cur = 0;
         if (t < t_end) {
-            cx = __fsub_rn(__fmaf_rn(alpha, rx0, sx), 1.0f);
-            cy = __fsub_rn(__fmaf_rn(alpha, ry0, sy), 1.0f);
+            c2 = sub2_rn(fma2_rn(a2, r2, s2), one2);
             cz = __fsub_rn(__fmaf_rn(alpha, rz0, sz), 1.0f);
-            cbx = floorf(cx);
-            cby = floorf(cy);
+            cb2 = make_float2(floorf(c2.x), floorf(c2.y));
             cbz = floorf(cz);
-            w_cur = fetch_label_code(V, cbx, cby, cbz);
+            w_cur = fetch_label_code(V, cb2.x, cb2.y, cbz);
         }
         // `half` is std::true_type for the trapezoid half-weight samples, std::false_type otherwise:
         // a full-weight sample's weight 1 * rho is rho, so no multiply is issued for it
         auto sample = [&](auto half) {
-            const float an = __fadd_rn(alpha, step);
-            const float nx = __fsub_rn(__fmaf_rn(an, rx0, sx), 1.0f);
-            const float ny = __fsub_rn(__fmaf_rn(an, ry0, sy), 1.0f);
-            const float nz = __fsub_rn(__fmaf_rn(an, rz0, sz), 1.0f);
-            const float nbx = floorf(nx), nby = floorf(ny), nbz = floorf(nz);
-            const uint32_t w_next = fetch_label_code(V, nbx, nby, nbz);
-            const float px = cx, py = cy, pz = cz;
-            const float fx = __fsub_rn(px, cbx), fy = __fsub_rn(py, cby), fz = __fsub_rn(pz, cbz);
+            const float2 an2 = add2_rn(a2, step2);
+            const float2 n2 = sub2_rn(fma2_rn(an2, r2, s2), one2);
+            const float nz = __fsub_rn(__fmaf_rn(an2.x, rz0, sz), 1.0f);
+            const float2 nb2 = make_float2(floorf(n2.x), floorf(n2.y));
+            const float nbz = floorf(nz);
+            const uint32_t w_next = fetch_label_code(V, nb2.x, nb2.y, nbz);
+            const float2 f2 = sub2_rn(c2, cb2);
+            const float fz = __fsub_rn(cz, cbz);
             const uint32_t code = w_cur;
             const int uni_label = (code & (kCodeGeneral | 0xFF00u)) == 0u ? (int)(code & 15u) : -1;
-            const CornerWeights cw = corner_weights(fx, fy, fz);
-            const float rho = tex3D<float>(V.density, __fadd_rn(px, 0.5f), __fadd_rn(py, 0.5f), __fadd_rn(pz, 0.5f));
+            const float2 g2 = sub2_rn(one2, f2);
+            CornerWeights cw;
+            cw.xy[0] = __fmul_rn(g2.x, g2.y);
+            cw.xy[1] = __fmul_rn(f2.x, g2.y);
+            cw.xy[2] = __fmul_rn(g2.x, f2.y);
+            cw.xy[3] = __fmul_rn(f2.x, f2.y);
+            cw.z[0] = __fsub_rn(1.0f, fz);
+            cw.z[1] = fz;
+            const float2 tc2 = add2_rn(c2, half2v);
+            const float rho = tex3D<float>(V.density, tc2.x, tc2.y, __fadd_rn(cz, 0.5f));
             const float wr = decltype(half)::value ? __fmul_rn(0.5f, rho) : rho;
             if (uni_label >= 0) {
                 const float s = uniform_sum(cw);
@@ -566,15 +605,16 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
                     for (int m = 0; m < M; m++)
                         ad[m] = __fmaf_rn(wr, (uint32_t)m == A ? sA : ((uint32_t)m == B ? sB : 0.0f), ad[m]);
                 } else {
-                    word = general_label_word(V, cbx, cby, cbz);  // three or more labels: the corners' own
+                    word = general_label_word(V, cb2.x, cb2.y, cbz);  // three or more labels: the corners' own
                     float seg[M];
                     label_fractions<M>(word, cw, seg);
 #pragma unroll
                     for (int m = 0; m < M; m++) ad[m] = __fmaf_rn(wr, seg[m], ad[m]);
                 }
             }
-            alpha = an;
-            cx = nx, cy = ny, cz = nz, cbx = nbx, cby = nby, cbz = nbz;
+            a2 = an2;
+            alpha = an2.x;
+            c2 = n2, cz = nz, cb2 = nb2, cbz = nbz;
             w_cur = w_next;
         };
         if (t < t_end && t == 0) {
@@ -801,22 +841,37 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
             for (int i = 1; i < NV; i++)
                 if (i == v) vsx = view.vol[i].s[0], vsy = view.vol[i].s[1], vsz = view.vol[i].s[2];
             const VolConst &Vv = p.vol[v];
-            // n = 1 and full-weight samples: the weight fl(1 / 1) * rho is rho itself
-            float cx = __fsub_rn(__fmaf_rn(alpha, vrx, vsx), 1.0f);
-            float cy = __fsub_rn(__fmaf_rn(alpha, vry, vsy), 1.0f);
+            // n = 1 and full-weight samples: the weight fl(1 / 1) * rho is rho itself. x and y travel
+            // as f32x2 pairs, as in the single-volume march.
+            const float2 vr2 = make_float2(vrx, vry), vs2 = make_float2(vsx, vsy);
+            const float2 one2 = make_float2(1.0f, 1.0f), half2v = make_float2(0.5f, 0.5f);
+            const float2 step2 = make_float2(step, step);
+            float2 a2 = make_float2(alpha, alpha);
+            float2 c2 = sub2_rn(fma2_rn(a2, vr2, vs2), one2);
             float cz = __fsub_rn(__fmaf_rn(alpha, vrz, vsz), 1.0f);
-            float cbx = floorf(cx), cby = floorf(cy), cbz = floorf(cz);
+            float2 cb2 = make_float2(floorf(c2.x), floorf(c2.y));
+            float cbz = floorf(cz);
             // label codes, loaded a step ahead (the coincidence-free stretch needs no cache key)
-            uint32_t c_cur = fetch_label_code(Vv, cbx, cby, cbz);
+            uint32_t c_cur = fetch_label_code(Vv, cb2.x, cb2.y, cbz);
             for (int k = 0; k < kk; k++) {
-                const float an = __fadd_rn(alpha, step);
-                const float nx = __fsub_rn(__fmaf_rn(an, vrx, vsx), 1.0f);
-                const float ny = __fsub_rn(__fmaf_rn(an, vry, vsy), 1.0f);
-                const float nz = __fsub_rn(__fmaf_rn(an, vrz, vsz), 1.0f);
-                const float nbx = floorf(nx), nby = floorf(ny), nbz = floorf(nz);
-                const uint32_t c_next = fetch_label_code(Vv, nbx, nby, nbz);
-                const CornerWeights cw = corner_weights(__fsub_rn(cx, cbx), __fsub_rn(cy, cby), __fsub_rn(cz, cbz));
-                const float rho = tex3D<float>(Vv.density, __fadd_rn(cx, 0.5f), __fadd_rn(cy, 0.5f), __fadd_rn(cz, 0.5f));
+                const float2 an2 = add2_rn(a2, step2);
+                const float2 n2 = sub2_rn(fma2_rn(an2, vr2, vs2), one2);
+                const float nz = __fsub_rn(__fmaf_rn(an2.x, vrz, vsz), 1.0f);
+                const float2 nb2 = make_float2(floorf(n2.x), floorf(n2.y));
+                const float nbz = floorf(nz);
+                const uint32_t c_next = fetch_label_code(Vv, nb2.x, nb2.y, nbz);
+                const float2 f2 = sub2_rn(c2, cb2);
+                const float fz = __fsub_rn(cz, cbz);
+                const float2 g2 = sub2_rn(one2, f2);
+                CornerWeights cw;
+                cw.xy[0] = __fmul_rn(g2.x, g2.y);
+                cw.xy[1] = __fmul_rn(f2.x, g2.y);
+                cw.xy[2] = __fmul_rn(g2.x, f2.y);
+                cw.xy[3] = __fmul_rn(f2.x, f2.y);
+                cw.z[0] = __fsub_rn(1.0f, fz);
+                cw.z[1] = fz;
+                const float2 tc2 = add2_rn(c2, half2v);
+                const float rho = tex3D<float>(Vv.density, tc2.x, tc2.y, __fadd_rn(cz, 0.5f));
                 const float wr = rho;
                 if ((c_cur & (kCodeGeneral | 0xFF00u)) == 0u) {
                     const int L = (int)(c_cur & 15u);
@@ -845,14 +900,15 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
                             ad[m] = __fmaf_rn(wr, (uint32_t)m == A ? sA : ((uint32_t)m == B ? sB : 0.0f), ad[m]);
                     } else {
                         float seg[M];
-                        label_fractions<M>(general_label_word(Vv, cbx, cby, cbz), cw, seg);
+                        label_fractions<M>(general_label_word(Vv, cb2.x, cb2.y, cbz), cw, seg);
 #pragma unroll
                         for (int m = 0; m < M; m++) ad[m] = __fmaf_rn(wr, seg[m], ad[m]);
                     }
                 }
                 alpha_prev = alpha;
-                alpha = an;
-                cx = nx, cy = ny, cz = nz, cbx = nbx, cby = nby, cbz = nbz;
+                alpha = an2.x;
+                a2 = an2;
+                c2 = n2, cz = nz, cb2 = nb2, cbz = nbz;
                 c_cur = c_next;
             }
             pre_ok = 0u;  // the words of the next step are loaded by msample
