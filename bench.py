@@ -176,10 +176,15 @@ def scene_volumes(vols, mats):
     return [dict(density=v.data, labels=remapped_labels(v, mats), ijk_from_world=v.ijk_from_world.data) for v in vols]
 
 
+FORWARD_SOURCES = ("drr_forward.cuh", "drr_launch.cuh", "drr_alpha.h", "drr_coincide.h", "drr_inst_nv1.cu",
+                   "drr_inst_nv2.cu", "drr_inst_nv3.cu", "drr_inst_nv4.cu")
+
+
 def source_sha() -> str:
-    """Hash of the kernel sources, to tell whether a saved ncu figure still describes this build."""
+    """Hash of the forward kernel's sources (the files its instantiation units compile from), to tell
+    whether a saved ncu figure of that kernel still describes this build."""
     h = hashlib.sha256()
-    for p in sorted((ROOT / "deepdrr_gb300" / "csrc").glob("*.cu*")) + sorted((ROOT / "deepdrr_gb300" / "csrc").glob("*.h")):
+    for p in sorted(ROOT / "deepdrr_gb300" / "csrc" / name for name in FORWARD_SOURCES):
         h.update(p.name.encode())
         h.update(p.read_bytes())
     return h.hexdigest()[:16]

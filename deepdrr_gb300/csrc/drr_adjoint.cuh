@@ -19,8 +19,10 @@
 // float32 alpha sequence, same live step range, same trapezoid half weights); the 32 rays of a warp
 // step together. A ray's full-weight samples fall into runs: stretches with one label cell and one
 // texture-filter cell (the two half-weight samples are runs of their own). Within a run the
-// per-sample work is small and identical across the warp: the eight integer corner weights are
-// summed two to a register (drr_texweights.h). When a run ends, the ray appends its first alpha,
+// per-sample work is small and identical across the warp: the three staged terms of the eight
+// integer corner weights, two 16-bit lanes to a register, are summed, and the run's summed corner
+// weights are formed from them once (drr_texweights.h). A run ends where a sample's cells differ
+// from the previous sample's. When a run ends, the ray appends its first alpha,
 // length and sums to a per-warp ring in shared memory; once 32 runs wait, the warp drains them,
 // one run per lane, so the per-cell work -- the label word, eight texel additions to the gradient
 // volume, eight texel fetches and the pose sums -- runs with all lanes busy instead of once per
@@ -168,20 +170,23 @@ __device__ __forceinline__ bool adjoint_setup(const AdjointParams &P, const Adjo
     return R.t < R.t_end;
 }
 
-// Per-warp run queue of adjoint_kernel: a ring of kAdjQueue entries (structure of arrays, word k
-// of entry e at [k][e]); the warp drains 32 runs at a time.
+// Per-warp run queue of adjoint_kernel: a ring of kAdjQueue entries; the warp drains 32 runs at a
+// time. An entry is one 16-byte and one 8-byte word group: alpha0, count | lane << 8 | half << 13,
+// and the run's sums of the staged weight terms (SX, S0 | S1, SZ, drr_texweights.h). Past the ring,
+// one slot per lane takes the stores of lanes that close no run, so a push needs no branch.
 constexpr int kAdjQueue = 64;
-constexpr int kRunWords = 6;  // alpha0, count | lane << 8 | half << 13, four packed corner sums
 constexpr int kMixWords = 3;  // alpha0, count | lane << 8 | half << 13, label word
 
 template <int M>
 struct AdjointWarpSmem {
-    uint32_t run[kRunWords][kAdjQueue];
+    uint4 runa[kAdjQueue + 32];  // alpha0, count | lane << 8 | half << 13, SX, S0
+    uint2 runb[kAdjQueue + 32];  // S1, SZ
     uint32_t mix[kMixWords][kAdjQueue];  // runs in cells with mixed labels, set aside by the drain
     float gr[M][32];   // each lane's material weights gr_m
-    float ray[9][32];  // each lane's unit ray in IJK (0-2), source in IJK (3-5), unit ray in world (6-8)
-    float pose[6][32];  // each lane's share of the drained h sums (IJK, 0-2); each ray's hk sum (IJK, 3-5)
+    float ray[6][32];  // each lane's unit ray in IJK (0-2) and source in IJK (3-5)
+    float pose[6][32];  // each lane's share of the drained sums: h (IJK, 0-2) and the moments m (3-5)
     float A[9];        // the view's IJK_from_world rotation
+    float G[6];        // A A^T: xx, xy, xz, yy, yz, zz
 };
 
 __device__ __forceinline__ void red_add_pair(float *a, float x, float y) {
@@ -246,17 +251,23 @@ __device__ __forceinline__ int hw_fix_live(float p) {
     return (int)__float2uint_rd(__fmaf_rn(__fadd_rn(p, 0.5f), 256.0f, -127.5f));
 }
 
-// Pose sums of one run or sample: the IJK sum h into lane `lane`'s share, and the alpha-weighted sum
-// hk into the owner ray's own sum. The moment r x (A^T hk) is linear in hk and r is the owner's, so
-// it is taken once per ray at the end instead of once per run; lanes of one warp may add to the same
-// owner in one drain, hence the shared-memory atomics.
+// Pose sums of one run or sample, into lane `lane`'s own share: the IJK sum h, and the moment of
+// the alpha-weighted sum hk about the source, r x (A^T hk) in world coordinates (r the owner ray's
+// unit direction). With r_ijk = A r and any invertible A, (A^-1 a) x (A^-1 b) = A^T (a x b) / det A
+// gives r x (A^T hk) = A^T (r_ijk x (A A^T hk)) / det A: the lane sums m = r_ijk x (G hk), G = A A^T,
+// and A^T / det A is applied once per warp at the end. No lane writes another lane's share, so no
+// atomics are needed (shared-memory float atomics cost more than the twelve multiply-adds).
 template <int M>
 __device__ __forceinline__ void add_pose_sums(AdjointWarpSmem<M> &sh, int lane, const float h[3], const float hk[3],
                                               int owner) {
     sh.pose[0][lane] += h[0], sh.pose[1][lane] += h[1], sh.pose[2][lane] += h[2];
-    atomicAdd(&sh.pose[3][owner], hk[0]);
-    atomicAdd(&sh.pose[4][owner], hk[1]);
-    atomicAdd(&sh.pose[5][owner], hk[2]);
+    const float u0 = sh.G[0] * hk[0] + sh.G[1] * hk[1] + sh.G[2] * hk[2];
+    const float u1 = sh.G[1] * hk[0] + sh.G[3] * hk[1] + sh.G[4] * hk[2];
+    const float u2 = sh.G[2] * hk[0] + sh.G[4] * hk[1] + sh.G[5] * hk[2];
+    const float r0 = sh.ray[0][owner], r1 = sh.ray[1][owner], r2 = sh.ray[2][owner];
+    sh.pose[3][lane] += r1 * u2 - r2 * u1;
+    sh.pose[4][lane] += r2 * u0 - r0 * u2;
+    sh.pose[5][lane] += r0 * u1 - r1 * u0;
 }
 
 // One sample of a mixed-label cell at float32 alpha `al` of ray `owner` (label word `word`): the
@@ -367,11 +378,10 @@ __device__ __forceinline__ void drain_mixed(const AdjointParams &P, AdjointWarpS
 // each warp 8 x 4 pixels). A run is a stretch of a ray's full-weight samples with one label cell
 // and one texture-filter cell; the trapezoid half-weight samples (t = 0 and t = num_steps - 1) are
 // runs of their own. See the file comment. Resident blocks per SM balance occupancy against the
-// registers the drain needs: measured with 3 materials, 6 blocks (80 registers, a few spills)
-// against 5 (96): 1.59 against 1.60 ms/view forward + backward; 7 and 8 blocks spill more and
-// are slower. More materials keep 5.
+// registers the drain needs: with 3 materials, 7 blocks (72 registers, no spills) measured 0.888
+// ms/view against 0.906 at 6 blocks on the 256^3 / 64 x 256^2 workload. More materials keep 5.
 template <int M>
-__global__ void __launch_bounds__(kBlockThreads, M <= 4 ? 6 : 5) adjoint_kernel(const __grid_constant__ AdjointParams P) {
+__global__ void __launch_bounds__(kBlockThreads, M <= 4 ? 7 : 5) adjoint_kernel(const __grid_constant__ AdjointParams P) {
     __shared__ AdjointWarpSmem<M> smem[kBlockThreads / 32];
     const SceneParams<1> &p = P.s;
     const int lane = threadIdx.x & 31;
@@ -396,10 +406,13 @@ __global__ void __launch_bounds__(kBlockThreads, M <= 4 ? 6 : 5) adjoint_kernel(
     sh.ray[3][lane] = R.sx;
     sh.ray[4][lane] = R.sy;
     sh.ray[5][lane] = R.sz;
-    sh.ray[6][lane] = R.rx;
-    sh.ray[7][lane] = R.ry;
-    sh.ray[8][lane] = R.rz;
     if (lane < 9) sh.A[lane] = av.v.vol[0].a[lane];
+    __syncwarp();
+    if (lane < 6) {  // G = A A^T, entry (gi, gj)
+        const int gi = lane < 3 ? 0 : (lane < 5 ? 1 : 2), gj = lane < 3 ? lane : (lane < 5 ? lane - 2 : 2);
+        sh.G[lane] = sh.A[3 * gi] * sh.A[3 * gj] + sh.A[3 * gi + 1] * sh.A[3 * gj + 1] +
+                     sh.A[3 * gi + 2] * sh.A[3 * gj + 2];
+    }
     __syncwarp();
 
     const int n0 = V.n[0], n1 = V.n[1], n2 = V.n[2];
@@ -423,11 +436,13 @@ __global__ void __launch_bounds__(kBlockThreads, M <= 4 ? 6 : 5) adjoint_kernel(
         const int e = (first + lane) & (kAdjQueue - 1);
         float al = 0.0f, wrun = 1.0f;
         int kn = 0, owner = 0;
-        uint32_t word = 0;
+        uint32_t word = 0, w1 = 0;
         bool mixed = false;
         if (mine) {
-            al = __uint_as_float(sh.run[0][e]);
-            const uint32_t w1 = sh.run[1][e];
+            const uint4 ra = sh.runa[e];
+            const uint2 rb = sh.runb[e];
+            al = __uint_as_float(ra.x);
+            w1 = ra.y;
             kn = (int)(w1 & 255u), owner = (int)((w1 >> 8) & 31u);
             wrun = (w1 >> 13) & 1u ? 0.5f : 1.0f;
             const float rxi = sh.ray[0][owner], ryi = sh.ray[1][owner], rzi = sh.ray[2][owner];
@@ -446,7 +461,8 @@ __global__ void __launch_bounds__(kBlockThreads, M <= 4 ? 6 : 5) adjoint_kernel(
                 if (do_dens) {
                     // every sample adds w_t gu W_c / 256 to texel c: the packed sums hold sum W_c
                     const float rv = __fmul_rn(__fmul_rn(wrun, gu), 1.0f / 256.0f);
-                    const uint32_t sums[4] = {sh.run[2][e], sh.run[3][e], sh.run[4][e], sh.run[5][e]};
+                    uint32_t sums[4];
+                    packed_weight_sums((uint32_t)kn, ra.z, ra.w, rb.x, rb.y, sums);
                     float vals[8];
                     weighted_corners(sums, rv, vals);
                     scatter_cell(grad, hw_fix(px, n0) >> 8, hw_fix(py, n1) >> 8, hw_fix(pz, n2) >> 8, n0, n1, n2,
@@ -506,7 +522,7 @@ __global__ void __launch_bounds__(kBlockThreads, M <= 4 ? 6 : 5) adjoint_kernel(
         if (mixed) {
             const int s = (mhead + mqueued + __popc(mm & lt)) & (kAdjQueue - 1);
             sh.mix[0][s] = __float_as_uint(al);
-            sh.mix[1][s] = sh.run[1][e];
+            sh.mix[1][s] = w1;
             sh.mix[2][s] = word;
         }
         mqueued += __popc(mm);
@@ -527,23 +543,22 @@ __global__ void __launch_bounds__(kBlockThreads, M <= 4 ? 6 : 5) adjoint_kernel(
     const bool last_half = ray_live && R.t_end == R.num_steps && R.num_steps > 1;
     const int t_stop = last_half ? R.num_steps - 1 : R.t_end;  // end of the full-weight samples
 
-    // the open run: sample count, first alpha, label cell, filter fixed point, packed sums
+    // the open run: sample count, first alpha, sums of the staged weight terms hx, hy0, hy1 and of
+    // Az (drr_texweights.h); the label cell and filter fixed point of the previous sample
     int K = 0;
     float a0 = 0.0f, rbx = 0.0f, rby = 0.0f, rbz = 0.0f;
     int rfx = 0, rfy = 0, rfz = 0;
-    uint32_t S0 = 0, S1 = 0, S2 = 0, S3 = 0;
+    uint32_t SX = 0, S0 = 0, S1 = 0, SZ = 0;
 
     auto enqueue = [&](bool push, bool half) {
         const unsigned pm = __ballot_sync(kAll, push);
-        if (push) {
-            const int s = (head + queued + __popc(pm & lt)) & (kAdjQueue - 1);
-            sh.run[0][s] = __float_as_uint(a0);
-            sh.run[1][s] = (uint32_t)K | ((uint32_t)lane << 8) | (half ? 1u << 13 : 0u);
-            sh.run[2][s] = S0;
-            sh.run[3][s] = S1;
-            sh.run[4][s] = S2;
-            sh.run[5][s] = S3;
-            K = 0;
+        {
+            // a lane that closes no run stores into its own slot past the ring
+            const int s = push ? (head + queued + __popc(pm & lt)) & (kAdjQueue - 1) : kAdjQueue + lane;
+            sh.runa[s] = make_uint4(__float_as_uint(a0), (uint32_t)K | ((uint32_t)lane << 8) | (half ? 1u << 13 : 0u),
+                                    SX, S0);
+            sh.runb[s] = make_uint2(S1, SZ);
+            K = push ? 0 : K;
         }
         queued += __popc(pm);
         if (queued >= 32) {
@@ -560,14 +575,14 @@ __global__ void __launch_bounds__(kBlockThreads, M <= 4 ? 6 : 5) adjoint_kernel(
             const float cx = __fsub_rn(__fmaf_rn(alpha, R.rxi, R.sx), 1.0f);
             const float cy = __fsub_rn(__fmaf_rn(alpha, R.ryi, R.sy), 1.0f);
             const float cz = __fsub_rn(__fmaf_rn(alpha, R.rzi, R.sz), 1.0f);
-            uint32_t Wp[4] = {0u, 0u, 0u, 0u};
+            SX = S0 = S1 = SZ = 0u;
             if (do_dens) {
                 const int fxi = hw_fix(cx, n0), fyi = hw_fix(cy, n1), fzi = hw_fix(cz, n2);
-                packed_corner_weights((uint32_t)fxi & 255u, (uint32_t)fyi & 255u, (uint32_t)fzi & 255u, Wp);
+                SZ = (uint32_t)fzi & 255u;
+                weight_terms((uint32_t)fxi & 255u, (uint32_t)fyi & 255u, SZ, SX, S0, S1);
             }
             a0 = alpha;
             K = 1;
-            S0 = Wp[0], S1 = Wp[1], S2 = Wp[2], S3 = Wp[3];
         }
         enqueue(here, true);
     };
@@ -579,9 +594,13 @@ __global__ void __launch_bounds__(kBlockThreads, M <= 4 ? 6 : 5) adjoint_kernel(
     }
     // The warp runs its longest ray's full-weight samples plus one step that closes the last runs,
     // a bound known up front (one reduction), so the loop needs no vote per step. A lane past its
-    // own samples computes positions it does not use; its run state changes only through selects.
+    // own samples marches on through positions it does not use: it closes its last run, opens no
+    // other, and its sums are never queued again. Its alpha after its own samples, where the last
+    // half-weight sample lies, comes from the exact fast-forward (drr_alpha.h).
     const int my_steps = t < t_stop ? t_stop - t : 0;
     const int warp_steps = __reduce_max_sync(kAll, my_steps) + 1;
+    float alpha_end = alpha;
+    advance_alpha(&alpha_end, step, __int_as_float(0x7f800000), my_steps, false);
     float cx = __fsub_rn(__fmaf_rn(alpha, R.rxi, R.sx), 1.0f);
     float cy = __fsub_rn(__fmaf_rn(alpha, R.ryi, R.sy), 1.0f);
     float cz = __fsub_rn(__fmaf_rn(alpha, R.rzi, R.sz), 1.0f);
@@ -590,6 +609,9 @@ __global__ void __launch_bounds__(kBlockThreads, M <= 4 ? 6 : 5) adjoint_kernel(
         const bool live = it < my_steps;
         const float bx = floorf(cx), by = floorf(cy), bz = floorf(cz);
         int fxi = 0, fyi = 0, fzi = 0;
+        // Each axis's position, label cell and fixed point are monotone in alpha (every operation
+        // producing them is a monotone rounding), so a sample whose cells equal the previous
+        // sample's has the cells of the whole open run: comparing with the previous sample suffices.
         bool fresh = K == 0 || K == 255 || bx != rbx || by != rby || bz != rbz;
         if (do_dens) {
             fxi = hw_fix_live(cx), fyi = hw_fix_live(cy), fzi = hw_fix_live(cz);
@@ -599,24 +621,25 @@ __global__ void __launch_bounds__(kBlockThreads, M <= 4 ? 6 : 5) adjoint_kernel(
         enqueue(K > 0 && (!live || fresh), false);
         const bool open = live && K == 0;  // this sample starts a run
         a0 = open ? alpha : a0;
-        rbx = open ? bx : rbx, rby = open ? by : rby, rbz = open ? bz : rbz;
-        rfx = open ? fxi : rfx, rfy = open ? fyi : rfy, rfz = open ? fzi : rfz;
         if (do_dens) {
-            uint32_t Wp[4];
-            packed_corner_weights((uint32_t)fxi & 255u, (uint32_t)fyi & 255u, (uint32_t)fzi & 255u, Wp);
+            uint32_t hx, hy0, hy1;
+            const uint32_t Az = (uint32_t)fzi & 255u;
+            weight_terms((uint32_t)fxi & 255u, (uint32_t)fyi & 255u, Az, hx, hy0, hy1);
             // a lane past its samples adds to sums that are never queued again (its run is closed)
-            S0 = (open ? 0u : S0) + Wp[0];
-            S1 = (open ? 0u : S1) + Wp[1];
-            S2 = (open ? 0u : S2) + Wp[2];
-            S3 = (open ? 0u : S3) + Wp[3];
+            SX = (open ? 0u : SX) + hx;
+            S0 = (open ? 0u : S0) + hy0;
+            S1 = (open ? 0u : S1) + hy1;
+            SZ = (open ? 0u : SZ) + Az;
         }
+        rbx = bx, rby = by, rbz = bz;
+        rfx = fxi, rfy = fyi, rfz = fzi;
         K += live ? 1 : 0;
-        t += live ? 1 : 0;
-        alpha = live ? __fadd_rn(alpha, step) : alpha;
+        alpha = __fadd_rn(alpha, step);
         cx = __fsub_rn(__fmaf_rn(alpha, R.rxi, R.sx), 1.0f);
         cy = __fsub_rn(__fmaf_rn(alpha, R.ryi, R.sy), 1.0f);
         cz = __fsub_rn(__fmaf_rn(alpha, R.rzi, R.sz), 1.0f);
     }
+    alpha = alpha_end;
     single(last_half);
     __syncwarp();
     drain(head, queued);
@@ -627,17 +650,7 @@ __global__ void __launch_bounds__(kBlockThreads, M <= 4 ? 6 : 5) adjoint_kernel(
         // the warp's pose sums: each ray's moment r x (A^T hk), then one atomic per component
         __syncwarp();
         float Hs0 = sh.pose[0][lane], Hs1 = sh.pose[1][lane], Hs2 = sh.pose[2][lane];
-        float Cs0, Cs1, Cs2;
-        {
-            const float h0 = sh.pose[3][lane], h1 = sh.pose[4][lane], h2 = sh.pose[5][lane];
-            const float kx = sh.A[0] * h0 + sh.A[3] * h1 + sh.A[6] * h2;
-            const float ky = sh.A[1] * h0 + sh.A[4] * h1 + sh.A[7] * h2;
-            const float kz = sh.A[2] * h0 + sh.A[5] * h1 + sh.A[8] * h2;
-            const float ox = sh.ray[6][lane], oy = sh.ray[7][lane], oz = sh.ray[8][lane];
-            Cs0 = oy * kz - oz * ky;
-            Cs1 = oz * kx - ox * kz;
-            Cs2 = ox * ky - oy * kx;
-        }
+        float Cs0 = sh.pose[3][lane], Cs1 = sh.pose[4][lane], Cs2 = sh.pose[5][lane];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             Hs0 += __shfl_xor_sync(kAll, Hs0, o);
@@ -649,6 +662,15 @@ __global__ void __launch_bounds__(kBlockThreads, M <= 4 ? 6 : 5) adjoint_kernel(
         }
         if (lane == 0) {
             const float *A = sh.A;
+            {  // the rays' moments in world coordinates: A^T (sum of m) / det A
+                const float det = A[0] * (A[4] * A[8] - A[5] * A[7]) - A[1] * (A[3] * A[8] - A[5] * A[6]) +
+                                  A[2] * (A[3] * A[7] - A[4] * A[6]);
+                const float id = 1.0f / det;
+                const float m0 = Cs0, m1 = Cs1, m2 = Cs2;
+                Cs0 = id * (A[0] * m0 + A[3] * m1 + A[6] * m2);
+                Cs1 = id * (A[1] * m0 + A[4] * m1 + A[7] * m2);
+                Cs2 = id * (A[2] * m0 + A[5] * m1 + A[8] * m2);
+            }
             const float Hw[3] = {A[0] * Hs0 + A[3] * Hs1 + A[6] * Hs2, A[1] * Hs0 + A[4] * Hs1 + A[7] * Hs2,
                                  A[2] * Hs0 + A[5] * Hs1 + A[8] * Hs2};
             const float d[3] = {av.source_world[0] - P.center[0], av.source_world[1] - P.center[1],

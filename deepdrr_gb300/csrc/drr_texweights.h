@@ -12,6 +12,8 @@
 // all eight with two 16-bit lanes per 32-bit word (dz = 0 in bits 0-15, dz = 1 in bits 16-31), so
 // one integer multiply-add serves both z planes. No lane can carry into the next: every product
 // plus rounding constant stays below 2^16 (checked for all 2^24 fractions by tests/test_texweights_cpu.py).
+// The march sums only the three staged terms and Az of each sample (weight_terms), and the sums of
+// the packed weights are formed once per run (packed_weight_sums).
 // Plain C++ so the same code runs in the kernel and in the CPU test.
 #pragma once
 
@@ -50,17 +52,45 @@ DRR_TW_HD void hw_corner_weights(int Ax, int Ay, int Az, int W[8]) {
     }
 }
 
+// (x >> 8) & 0x00FF00FF: the upper byte of each 16-bit lane moved down (one byte permute on the GPU).
+DRR_TW_HD uint32_t lane_high_bytes(uint32_t x) {
+#if defined(__CUDA_ARCH__)
+    return __byte_perm(x, 0u, 0x4341u);
+#else
+    return (x >> 8) & 0x00FF00FFu;
+#endif
+}
+
+// The staged terms of the packed weights: with vz = (256 - Az) | Az << 16, the dx = 1 column
+// hx = round-half-up(vz Ax / 256), and the dy = 1 parts of both columns, hy1 = round-half-up(hx Ay
+// / 256) and hy0 = round-half-down((vz - hx) Ay / 256), each lane-wise.
+DRR_TW_HD void weight_terms(uint32_t Ax, uint32_t Ay, uint32_t Az, uint32_t &hx, uint32_t &hy0, uint32_t &hy1) {
+    const uint32_t vz = 256u + Az * 65535u;  // (256 - Az) | Az << 16
+    hx = lane_high_bytes(vz * Ax + 0x00800080u);
+    hy1 = lane_high_bytes(hx * Ay + 0x00800080u);
+    hy0 = lane_high_bytes((vz - hx) * Ay + 0x007F007Fu);
+}
+
 // The same weights packed: P[dx * 2 + dy] = W[dx | dy << 1] | W[dx | dy << 1 | 4] << 16.
 DRR_TW_HD void packed_corner_weights(uint32_t Ax, uint32_t Ay, uint32_t Az, uint32_t P[4]) {
-    const uint32_t vz = 256u + Az * 65535u;                               // (256 - Az) | Az << 16
-    const uint32_t hx = ((vz * Ax + 0x00800080u) >> 8) & 0x00FF00FFu;     // dx = 1 column
-    const uint32_t vx0 = vz - hx;                                         // dx = 0 column
-    const uint32_t hy1 = ((hx * Ay + 0x00800080u) >> 8) & 0x00FF00FFu;    // round half up
-    const uint32_t hy0 = ((vx0 * Ay + 0x007F007Fu) >> 8) & 0x00FF00FFu;   // round half down
+    uint32_t hx, hy0, hy1;
+    weight_terms(Ax, Ay, Az, hx, hy0, hy1);
+    const uint32_t vx0 = 256u + Az * 65535u - hx;  // dx = 0 column
     P[0] = vx0 - hy0;  // dx 0, dy 0
     P[1] = hy0;        // dx 0, dy 1
     P[2] = hx - hy1;   // dx 1, dy 0
     P[3] = hy1;        // dx 1, dy 1
+}
+
+// The packed weights summed over k samples, from the sums of their staged terms (SX = sum hx,
+// S0 = sum hy0, S1 = sum hy1, SZ = sum Az): the sum of vz is 256 k + SZ * 65535, and every lane of
+// every sum stays below 2^16 for k <= 255, so the lane-wise subtractions borrow nothing.
+DRR_TW_HD void packed_weight_sums(uint32_t k, uint32_t SX, uint32_t S0, uint32_t S1, uint32_t SZ, uint32_t P[4]) {
+    const uint32_t vzs = 256u * k + SZ * 65535u;
+    P[0] = vzs - SX - S0;
+    P[1] = S0;
+    P[2] = SX - S1;
+    P[3] = S1;
 }
 
 }  // namespace drr

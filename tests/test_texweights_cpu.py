@@ -1,6 +1,7 @@
 """The adjoint's integer form of the texture unit's linear filter (deepdrr_gb300/csrc/drr_texweights.h):
-the packed two-lane corner weights against the staged scalar rule for every fraction triple, and
-the fused fixed-point coordinate against the clamp-then-round form on random and edge coordinates."""
+the packed two-lane corner weights against the staged scalar rule for every fraction triple, the
+run sums formed from the staged terms against the summed packed weights, and the fused fixed-point
+coordinate against the clamp-then-round form on random and edge coordinates."""
 import ctypes
 import subprocess
 from pathlib import Path
@@ -18,6 +19,7 @@ def shim(tmp_path_factory):
                            str(HERE / "texweights_shim.cpp"), "-o", str(out)])
     lib = ctypes.CDLL(str(out))
     lib.packed_mismatches.restype = ctypes.c_longlong
+    lib.term_mismatches.restype = ctypes.c_longlong
     for f in (lib.fix_kernel_form, lib.fix_staged_form):
         f.restype = ctypes.c_int
         f.argtypes = [ctypes.c_float, ctypes.c_int]
@@ -26,6 +28,10 @@ def shim(tmp_path_factory):
 
 def test_packed_weights_match_the_staged_rule_for_every_fraction(shim):
     assert shim.packed_mismatches() == 0
+
+
+def test_run_sums_from_the_staged_terms_equal_the_summed_packed_weights(shim):
+    assert shim.term_mismatches() == 0
 
 
 def test_fixed_point_coordinate_forms_agree(shim):

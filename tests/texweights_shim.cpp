@@ -50,3 +50,42 @@ extern "C" int fix_staged_form(float x, int n) {
     volatile float w = v + 0.5f;
     return (int)std::floor(w);
 }
+
+// Counts mismatches between the packed weights of runs of k samples summed directly and the same
+// sums formed from the staged terms (weight_terms, packed_weight_sums): every fraction triple as a
+// one-sample run, then runs of 2 to 255 samples of random, all-maximum and all-zero fractions.
+extern "C" long long term_mismatches(void) {
+    long long bad = 0;
+    auto run = [&](int k, const uint32_t *ax, const uint32_t *ay, const uint32_t *az) {
+        uint32_t want[4] = {0u, 0u, 0u, 0u}, SX = 0u, S0 = 0u, S1 = 0u, SZ = 0u;
+        for (int i = 0; i < k; i++) {
+            uint32_t P[4], hx, hy0, hy1;
+            drr::packed_corner_weights(ax[i], ay[i], az[i], P);
+            drr::weight_terms(ax[i], ay[i], az[i], hx, hy0, hy1);
+            for (int c = 0; c < 4; c++) want[c] += P[c];
+            SX += hx, S0 += hy0, S1 += hy1, SZ += az[i];
+        }
+        uint32_t got[4];
+        drr::packed_weight_sums((uint32_t)k, SX, S0, S1, SZ, got);
+        for (int c = 0; c < 4; c++)
+            if (got[c] != want[c]) ++bad;
+    };
+    for (uint32_t Az = 0; Az < 256; Az++)
+        for (uint32_t Ax = 0; Ax < 256; Ax++)
+            for (uint32_t Ay = 0; Ay < 256; Ay++) run(1, &Ax, &Ay, &Az);
+    uint32_t ax[255], ay[255], az[255];
+    uint64_t s = 0x9E3779B97F4A7C15ull;
+    for (int trial = 0; trial < 3000; trial++) {
+        const int k = 2 + trial % 254;
+        for (int i = 0; i < k; i++) {
+            s = s * 6364136223846793005ull + 1442695040888963407ull;
+            const uint32_t r = (uint32_t)(s >> 32);
+            const int mode = trial % 3;  // random, all maximum, all zero
+            ax[i] = mode == 1 ? 255u : (mode == 2 ? 0u : (r & 255u));
+            ay[i] = mode == 1 ? 255u : (mode == 2 ? 0u : ((r >> 8) & 255u));
+            az[i] = mode == 1 ? 255u : (mode == 2 ? 0u : ((r >> 16) & 255u));
+        }
+        run(k, ax, ay, az);
+    }
+    return bad;
+}
