@@ -193,14 +193,11 @@ __device__ __forceinline__ void red_add_pair(float *a, float x, float y) {
     if ((reinterpret_cast<uintptr_t>(a) & 7u) == 0) {
         asm volatile("red.global.add.v2.f32 [%0], {%1, %2};" ::"l"(a), "f"(x), "f"(y) : "memory");
     } else {
-        if (x != 0.0f) atomicAdd(a, x);
-        if (y != 0.0f) atomicAdd(a + 1, y);
+        atomicAdd(a, x);
+        atomicAdd(a + 1, y);
     }
 }
 
-// Adds v[c] to texel c = dx | dy << 1 | dz << 2 of the filter cell with lower corner (i0, j0, k0):
-// texel (min(i0 + dx, n0 - 1), ...) of the [n2][n1][n0] gradient volume, as the texture's clamp
-// addressing reads it. The two texels of a row are adjacent and go out as one vector reduction.
 // rv * W for the eight corner weights packed two to a word (P[dx * 2 + dy] = W(dz = 0) | W(dz = 1) << 16,
 // drr_texweights.h), ordered for scatter_cell (v[2 row + dx] with row = dy | dz << 1). A 16-bit count
 // becomes a float through the exponent field (2^23 + count is exact below 2^23), and one fused
@@ -219,8 +216,13 @@ __device__ __forceinline__ void weighted_corners(const uint32_t P[4], float rv, 
     }
 }
 
-// Volumes of at most 32767 texels per axis (drr_project_adjoint's limit) keep a plane's offsets below
-// 2^31, so the rows are addressed as a plane pointer (one widening multiply) plus 32-bit offsets.
+// Adds v[c] to texel c = dx | dy << 1 | dz << 2 of the filter cell with lower corner (i0, j0, k0):
+// texel (min(i0 + dx, n0 - 1), ...) of the [n2][n1][n0] gradient volume, as the texture's clamp
+// addressing reads it. The two texels of a row are adjacent and go out as one vector reduction.
+// Zero values are added too: a weight is zero only for a fraction of exactly 0, and testing for
+// it costs the warp more than the few extra reductions. Volumes of at most 32767 texels per axis
+// (drr_project_adjoint's limit) keep a plane's offsets below 2^31, so the rows are addressed as a
+// plane pointer (one widening multiply) plus 32-bit offsets.
 __device__ __forceinline__ void scatter_cell(float *grad, int i0, int j0, int k0, int n0, int n1, int n2,
                                              const float v[8]) {
     const int j1 = min(j0 + 1, n1 - 1), k1 = min(k0 + 1, n2 - 1);
@@ -232,8 +234,8 @@ __device__ __forceinline__ void scatter_cell(float *grad, int i0, int j0, int k0
         const float x = v[2 * row], y = v[2 * row + 1];
         float *a = (row & 2 ? p1 : p0) + (row & 1 ? o1 : o0);
         if (i0 + 1 >= n0) {  // clamped edge: both corners are the same texel
-            if (x + y != 0.0f) atomicAdd(a, x + y);
-        } else if (x != 0.0f || y != 0.0f) {
+            atomicAdd(a, x + y);
+        } else {
             red_add_pair(a, x, y);
         }
     }

@@ -105,7 +105,7 @@ void free_volume(Volume &v) {
 // Label codes of every base of a volume (see drr::pack_labels_kernel) and the labels as a uint8
 // texture, owned by the volume set: 2 bytes per base plus 1 byte per voxel.
 drr_status make_label_tables(const uint8_t *src, int ni, int nj, int nk, cudaStream_t s, Volume &v) {
-    const size_t np = (size_t)(ni + 1) * (nj + 1) * (nk + 1);
+    const size_t np = (size_t)(ni + 2) * (nj + 2) * (nk + 2);
     DRR_CUDA_TRY(cudaMalloc(&v.coded, np * sizeof(uint16_t)), "cudaMalloc (label codes)");
     const drr_status st = make_texture(src, 1, cudaCreateChannelDesc(8, 0, 0, 0, cudaChannelFormatKindUnsigned),
                                        false, ni, nj, nk, s, &v.labels_array, &v.labels_tex);
@@ -121,11 +121,11 @@ drr_status make_label_tables(const uint8_t *src, int ni, int nj, int nk, cudaStr
 
 namespace drr {
 __global__ void pack_labels_kernel(const uint8_t *__restrict__ labels, int ni, int nj, int nk, uint16_t *coded) {
-    const size_t np = (size_t)(ni + 1) * (nj + 1) * (nk + 1);
+    const size_t np = (size_t)(ni + 2) * (nj + 2) * (nk + 2);
     for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < np; e += (size_t)gridDim.x * blockDim.x) {
-        const int bi = (int)(e % (ni + 1)) - 1;
-        const int bj = (int)((e / (ni + 1)) % (nj + 1)) - 1;
-        const int bk = (int)(e / ((size_t)(ni + 1) * (nj + 1))) - 1;
+        const int bi = (int)(e % (ni + 2)) - 2;
+        const int bj = (int)((e / (ni + 2)) % (nj + 2)) - 2;
+        const int bk = (int)(e / ((size_t)(ni + 2) * (nj + 2))) - 2;
         uint32_t word = 0;
 #pragma unroll
         for (int c = 0; c < 8; c++) {

@@ -61,8 +61,8 @@ constexpr int kMaxSteps = 1 << 26;      // longest march per ray; longer rays ar
 
 struct VolConst {
     cudaTextureObject_t density;  // linear filter, clamp, unnormalised coordinates
-    const uint16_t *coded;        // label codes [(nk+1)][(nj+1)][(ni+1)] (pack_labels_kernel), at the entry of
-                                  // base (0, 0, 0): bases run from -1 to n - 1 on each axis
+    const uint16_t *coded;        // label codes [(nk+2)][(nj+2)][(ni+2)] (pack_labels_kernel), at the entry of
+                                  // base (0, 0, 0): bases run from -2 to n - 1 on each axis
     cudaTextureObject_t labels;   // the labels themselves (uint8, point filter, clamp), read for neighbourhoods
                                   // of three or more labels
     int32_t n[3];                 // ni, nj, nk
@@ -70,8 +70,8 @@ struct VolConst {
     float nm1[3];                 // n - 1 per axis
     int32_t priority;
     int32_t enabled;
-    int32_t row;          // code-table entries per row: n[0] + 1
-    int32_t plane_bytes;  // code-table bytes per plane: 2 (n[0] + 1)(n[1] + 1), below 2^31 because
+    int32_t row;          // code-table entries per row: n[0] + 2
+    int32_t plane_bytes;  // code-table bytes per plane: 2 (n[0] + 2)(n[1] + 2), below 2^31 because
                           // volumes are at most 16384 texels per axis (drr_volset_create)
 };
 
@@ -215,7 +215,7 @@ __device__ __forceinline__ int clampi(int x, int lo, int hi) { return x < lo ? l
 // here because p = F (-) 1 with F = fma(alpha, r, s) a float: for |p| <= 2, p (+) 1 is exact
 // (Sterbenz), and above that 1 is a multiple of ulp(p) (up to |p| = 2^24, far outside any volume,
 // where both corners clamp to the same texel anyway). So the neighbourhood is a function of the
-// base alone, precomputed per base b in [-1, n-1]^3 (pack_labels_kernel) as a 16-bit code:
+// base alone, precomputed per base b in [-2, n-1]^3 (pack_labels_kernel) as a 16-bit code:
 //   bits 0-3   A, corner 0's label
 //   bits 4-7   B, the other label of a two-label neighbourhood (A when there is none)
 //   bits 9-15  the corners 1-7 labelled B (bit 8 + c for corner c)
@@ -224,10 +224,13 @@ __device__ __forceinline__ int clampi(int x, int lo, int hi) { return x < lo ? l
 // So a neighbourhood is uniform when code >> 8 == 0.
 constexpr uint32_t kCodeGeneral = 0x100u;
 
-// Entry of base (i, j, k), -1 <= i <= n[0] - 1 etc., of a code table [(n[2]+1)][(n[1]+1)][(n[0]+1)]
+// Entry of base (i, j, k), -2 <= i <= n[0] - 1 etc., of a code table [(n[2]+2)][(n[1]+2)][(n[0]+2)]
 // given at the entry of base (0, 0, 0): the plane by one widening 32 x 32 -> 64-bit multiply, the
-// offset inside it in 32-bit arithmetic (|offset| < (n[0]+1)(n[1]+1) <= 16385^2). This is the address
-// of entry ((k+1)(n[1]+1) + j+1)(n[0]+1) + i+1 of the table's start, computed in 64 bits.
+// offset inside it in 32-bit arithmetic (|offset| < (n[0]+2)(n[1]+2) <= 16386^2). This is the address
+// of entry ((k+2)(n[1]+2) + j+2)(n[0]+2) + i+2 of the table's start, computed in 64 bits.
+// Base -2 holds the same neighbourhood as base -1 (on that axis both corners clamp to texel 0); the
+// extra layer lets marches whose bases provably stay in [-2, n-1] skip the clamps
+// (fetch_label_code_direct).
 __device__ __forceinline__ uint32_t label_entry(const uint16_t *origin, const VolConst &V, int i, int j, int k) {
     const char *plane = reinterpret_cast<const char *>(origin) + (long long)k * V.plane_bytes;
     return (uint32_t)__ldg(reinterpret_cast<const unsigned short *>(plane) + (j * V.row + i));
@@ -239,6 +242,23 @@ __device__ __forceinline__ uint32_t fetch_label_code(const VolConst &V, float bx
     const int j = (int)fminf(fmaxf(by, -1.0f), V.nm1[1]);
     const int k = (int)fminf(fmaxf(bz, -1.0f), V.nm1[2]);
     return label_entry(V.coded, V, i, j, k);
+}
+
+// The code of base b read without clamps: only for bases known to lie in [-2, n-1] on every axis,
+// where the table has an entry equal to the clamped base's (see direct_bases).
+__device__ __forceinline__ uint32_t fetch_label_code_direct(const VolConst &V, float bx, float by, float bz) {
+    return label_entry(V.coded, V, (int)bx, (int)by, (int)bz);
+}
+
+// Whether a march may read its label codes without clamps. Its samples' positions
+// fl(fl(fma(alpha, r, s)) - 1) and their floors are monotone in alpha on each axis (every operation
+// is a monotone rounding), so every base it meets lies between the bases of its first and its last
+// position (b0 and b1 here; the last is the look-ahead one step past its last sample, whose code
+// the march also loads). Written as comparisons so that a NaN fails.
+__device__ __forceinline__ bool direct_bases(const VolConst &V, float2 b0xy, float b0z, float2 b1xy, float b1z) {
+    return b0xy.x >= -2.0f && b1xy.x >= -2.0f && b0xy.x <= V.nm1[0] && b1xy.x <= V.nm1[0] &&
+           b0xy.y >= -2.0f && b1xy.y >= -2.0f && b0xy.y <= V.nm1[1] && b1xy.y <= V.nm1[1] &&
+           b0z >= -2.0f && b1z >= -2.0f && b0z <= V.nm1[2] && b1z <= V.nm1[2];
 }
 
 // The packed word of a neighbourhood of three or more labels, 4 bits per corner (corner c at bits
@@ -498,6 +518,7 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
     float alpha = minA;
     int t = 0;
     int t_end = num_steps;  // the march can stop here: no interval is open beyond it
+    float alpha_stop = alpha;  // alpha at step t_end (set with t_end below)
     const bool carve = p.hit_alpha != nullptr;  // subtractive meshes: the reference's full march
     if (!p.full_march && !carve) {
         // Skip the steps before any interval opens and stop after the last one closes; the float32
@@ -510,6 +531,7 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
             }
             float a_end = alpha;
             t_end = t + advance_alpha(&a_end, step, amax, num_steps - t, true);  // first alpha > amax
+            alpha_stop = a_end;
         } else {
             t = t_end = num_steps;  // no volume is ever sampled
         }
@@ -546,22 +568,31 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
         float2 c2 = make_float2(0.0f, 0.0f), cb2 = make_float2(0.0f, 0.0f);
         float cz = 0.0f, cbz = 0.0f;
         uint32_t w_cur = 0;
+        bool direct = false;  // every base of this march has a code-table entry without clamping
         if (t < t_end) {
             c2 = sub2_rn(fma2_rn(a2, r2, s2), one2);
             cz = __fsub_rn(__fmaf_rn(alpha, rz0, sz), 1.0f);
             cb2 = make_float2(floorf(c2.x), floorf(c2.y));
             cbz = floorf(cz);
             w_cur = fetch_label_code(V, cb2.x, cb2.y, cbz);
+            // the last position whose code the march loads: one step past its last sample, at step
+            // t_end, computed with the march's own operations
+            const float2 e2 = sub2_rn(fma2_rn(make_float2(alpha_stop, alpha_stop), r2, s2), one2);
+            const float ez = __fsub_rn(__fmaf_rn(alpha_stop, rz0, sz), 1.0f);
+            direct = direct_bases(V, cb2, cbz, make_float2(floorf(e2.x), floorf(e2.y)), floorf(ez));
         }
         // `half` is std::true_type for the trapezoid half-weight samples, std::false_type otherwise:
-        // a full-weight sample's weight 1 * rho is rho, so no multiply is issued for it
-        auto sample = [&](auto half) {
+        // a full-weight sample's weight 1 * rho is rho, so no multiply is issued for it. `dir` is
+        // std::true_type where the march's bases need no clamping (`direct`): six fewer operations
+        // per sample, the same codes.
+        auto sample = [&](auto half, auto dir) {
             const float2 an2 = add2_rn(a2, step2);
             const float2 n2 = sub2_rn(fma2_rn(an2, r2, s2), one2);
             const float nz = __fsub_rn(__fmaf_rn(an2.x, rz0, sz), 1.0f);
             const float2 nb2 = make_float2(floorf(n2.x), floorf(n2.y));
             const float nbz = floorf(nz);
-            const uint32_t w_next = fetch_label_code(V, nb2.x, nb2.y, nbz);
+            const uint32_t w_next = decltype(dir)::value ? fetch_label_code_direct(V, nb2.x, nb2.y, nbz)
+                                                         : fetch_label_code(V, nb2.x, nb2.y, nbz);
             const float2 f2 = sub2_rn(c2, cb2);
             const float fz = __fsub_rn(cz, cbz);
             const uint32_t code = w_cur;
@@ -617,19 +648,25 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
             c2 = n2, cz = nz, cb2 = nb2, cbz = nbz;
             w_cur = w_next;
         };
-        if (t < t_end && t == 0) {
-            sample(std::true_type{});
-            ++t;
-        }
-        const bool last_half = t < t_end && t_end == num_steps;
-        const int t_main = last_half ? t_end - 1 : t_end;
-        // two samples per iteration: the loop-carried position and word then need no moves
+        auto march = [&](auto dir) {
+            if (t < t_end && t == 0) {
+                sample(std::true_type{}, dir);
+                ++t;
+            }
+            const bool last_half = t < t_end && t_end == num_steps;
+            const int t_main = last_half ? t_end - 1 : t_end;
+            // two samples per iteration: the loop-carried position and word then need no moves
 #pragma unroll 2
-        for (; t < t_main; ++t) sample(std::false_type{});
-        if (last_half) {
-            sample(std::true_type{});
-            ++t;
-        }
+            for (; t < t_main; ++t) sample(std::false_type{}, dir);
+            if (last_half) {
+                sample(std::true_type{}, dir);
+                ++t;
+            }
+        };
+        if (direct)
+            march(std::true_type{});
+        else
+            march(std::false_type{});
         if (cur_m >= 0) store_ad<M>(ad, cur_m, cur_ad);
     } else if (NV > 1 && !p.full_march && !carve) {
         // Several volumes between the first interval's entry and the last one's exit: the
@@ -834,6 +871,8 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
             a = alpha;
             kk = min(kk, advance_alpha(&a, step, leave, kk, true));       // and not past the end
             if (kk < 2) return false;
+            // a is now the alpha one step past the stretch's last sample: the last position whose
+            // label code the stretch loads
             const int v = __ffs(adds) - 1;
             const float vrx = RXI(v), vry = RYI(v), vrz = RZI(v);
             float vsx = view.vol[0].s[0], vsy = view.vol[0].s[1], vsz = view.vol[0].s[2];
@@ -851,15 +890,21 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
             float cz = __fsub_rn(__fmaf_rn(alpha, vrz, vsz), 1.0f);
             float2 cb2 = make_float2(floorf(c2.x), floorf(c2.y));
             float cbz = floorf(cz);
-            // label codes, loaded a step ahead (the coincidence-free stretch needs no cache key)
+            // label codes, loaded a step ahead (the coincidence-free stretch needs no cache key);
+            // without clamps where every base of the stretch has a table entry (direct_bases)
             uint32_t c_cur = fetch_label_code(Vv, cb2.x, cb2.y, cbz);
+            const float2 e2 = sub2_rn(fma2_rn(make_float2(a, a), vr2, vs2), one2);
+            const float ez = __fsub_rn(__fmaf_rn(a, vrz, vsz), 1.0f);
+            const bool direct = direct_bases(Vv, cb2, cbz, make_float2(floorf(e2.x), floorf(e2.y)), floorf(ez));
+            auto stretch = [&](auto dir) {
             for (int k = 0; k < kk; k++) {
                 const float2 an2 = add2_rn(a2, step2);
                 const float2 n2 = sub2_rn(fma2_rn(an2, vr2, vs2), one2);
                 const float nz = __fsub_rn(__fmaf_rn(an2.x, vrz, vsz), 1.0f);
                 const float2 nb2 = make_float2(floorf(n2.x), floorf(n2.y));
                 const float nbz = floorf(nz);
-                const uint32_t c_next = fetch_label_code(Vv, nb2.x, nb2.y, nbz);
+                const uint32_t c_next = decltype(dir)::value ? fetch_label_code_direct(Vv, nb2.x, nb2.y, nbz)
+                                                             : fetch_label_code(Vv, nb2.x, nb2.y, nbz);
                 const float2 f2 = sub2_rn(c2, cb2);
                 const float fz = __fsub_rn(cz, cbz);
                 const float2 g2 = sub2_rn(one2, f2);
@@ -911,6 +956,11 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
                 c2 = n2, cz = nz, cb2 = nb2, cbz = nbz;
                 c_cur = c_next;
             }
+            };
+            if (direct)
+                stretch(std::true_type{});
+            else
+                stretch(std::false_type{});
             pre_ok = 0u;  // the words of the next step are loaded by msample
             tracking = false;
             t += kk;
@@ -1114,7 +1164,7 @@ __global__ void __launch_bounds__(kBlockThreads, forward_min_blocks<NV, M>()) fo
     }
 }
 
-// Codes the labels of every 2x2x2 neighbourhood: the code of base b in [-1, n-1]^3 describes the labels
+// Codes the labels of every 2x2x2 neighbourhood: the code of base b in [-2, n-1]^3 describes the labels
 // at clamp(b + d, 0, n - 1), corner c = dx | dy << 1 | dz << 2 (the layout above kCodeGeneral).
 __global__ void pack_labels_kernel(const uint8_t *__restrict__ labels, int ni, int nj, int nk, uint16_t *coded);
 

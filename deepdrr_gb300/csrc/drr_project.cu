@@ -64,8 +64,8 @@ void fill_scene(drr::SceneParams<NV> &p, const drr_volset *set, const drr_tables
     for (int i = 0; i < NV; i++) {
         const drr::Volume &v = set->vol[i];
         p.vol[i].density = v.density_tex;
-        // code table addressed from the entry of base (0, 0, 0): one plane, one row and one entry in
-        const size_t origin = (size_t)(v.ni + 1) * (size_t)(v.nj + 1) + (size_t)(v.ni + 1) + 1;
+        // code table addressed from the entry of base (0, 0, 0): two planes, two rows and two entries in
+        const size_t origin = 2 * ((size_t)(v.ni + 2) * (size_t)(v.nj + 2) + (size_t)(v.ni + 2) + 1);
         p.vol[i].coded = v.coded ? v.coded + origin : nullptr;
         p.vol[i].labels = v.labels_tex;
         p.vol[i].n[0] = v.ni;
@@ -77,8 +77,8 @@ void fill_scene(drr::SceneParams<NV> &p, const drr_volset *set, const drr_tables
         p.vol[i].hi[0] = (float)(v.ni - 0.5);
         p.vol[i].hi[1] = (float)(v.nj - 0.5);
         p.vol[i].hi[2] = (float)(v.nk - 0.5);
-        p.vol[i].row = v.ni + 1;
-        p.vol[i].plane_bytes = (int32_t)(2 * (int64_t)(v.ni + 1) * (int64_t)(v.nj + 1));
+        p.vol[i].row = v.ni + 2;
+        p.vol[i].plane_bytes = (int32_t)(2 * (int64_t)(v.ni + 2) * (int64_t)(v.nj + 2));
         p.vol[i].priority = a.priority[i];
         p.vol[i].enabled = a.enabled[i] ? 1 : 0;
     }
