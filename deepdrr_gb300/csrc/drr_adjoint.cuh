@@ -29,8 +29,11 @@
 // lane that happens to change cell. The drain re-derives a run's positions from its first alpha
 // with the march's own float32 operations. A run in a cell whose eight labels agree is summed in
 // closed form: q and Q are constant there and grad rho is bilinear in the fractions, so the pose
-// sums over the run's evenly spaced samples are polynomials in the run length. Runs in cells with
-// mixed labels wait in a second ring and are then split into their samples, 32 evaluated at once.
+// sums over the run's evenly spaced samples are polynomials in the run length; in a cell whose
+// eight texels are equal they are zero, and a drain whose 32 runs all lie in such cells (air of
+// constant density, which a warp's neighbouring rays often cross together) skips them. Runs in
+// cells with mixed labels wait in a second ring and are then split into their samples, 32
+// evaluated at once.
 // Only single-volume projections without air attenuation outside the volume are differentiated.
 #pragma once
 
@@ -170,17 +173,19 @@ __device__ __forceinline__ bool adjoint_setup(const AdjointParams &P, const Adjo
     return R.t < R.t_end;
 }
 
-// Per-warp run queue of adjoint_kernel: a ring of kAdjQueue entries; the warp drains 32 runs at a
-// time. An entry is one 16-byte and one 8-byte word group: alpha0, count | lane << 8 | half << 13,
-// and the run's sums of the staged weight terms (SX, S0 | S1, SZ, drr_texweights.h). Past the ring,
-// one slot per lane takes the stores of lanes that close no run, so a push needs no branch.
+// Per-warp run queues of adjoint_kernel: rings the warp drains 32 runs at a time (runs: kRunQueue
+// entries; runs set aside in mixed-label cells: kAdjQueue). A run entry is one 16-byte and one
+// 8-byte word group: alpha0, count | lane << 8 | half << 13, and the run's sums of the staged
+// weight terms (SX, S0 | S1, SZ, drr_texweights.h). Past the run ring, one slot per lane takes the
+// stores of lanes that close no run, so a push needs no branch.
 constexpr int kAdjQueue = 64;
+constexpr int kRunQueue = 128;  // run ring: up to 31 waiting + 64 pushed in two steps
 constexpr int kMixWords = 3;  // alpha0, count | lane << 8 | half << 13, label word
 
 template <int M>
 struct AdjointWarpSmem {
-    uint4 runa[kAdjQueue + 32];  // alpha0, count | lane << 8 | half << 13, SX, S0
-    uint2 runb[kAdjQueue + 32];  // S1, SZ
+    uint4 runa[kRunQueue + 32];  // alpha0, count | lane << 8 | half << 13, SX, S0
+    uint2 runb[kRunQueue + 32];  // S1, SZ
     uint32_t mix[kMixWords][kAdjQueue];  // runs in cells with mixed labels, set aside by the drain
     float gr[M][32];   // each lane's material weights gr_m
     float ray[6][32];  // each lane's unit ray in IJK (0-2) and source in IJK (3-5)
@@ -368,9 +373,22 @@ __device__ __forceinline__ void drain_mixed(const AdjointParams &P, AdjointWarpS
         const float s_w = __shfl_sync(kAll, wrun, src);
         const uint32_t s_word = __shfl_sync(kAll, word, src);
         if (g < total) {
+            // the march's float32 alpha sequence: k = g - o_prev (< 255) additions from the run's
+            // first. After the first addition every addition adds the same number of ulps while
+            // alpha stays in one binade (drr_alpha.h), so a_k = a_1 + (k - 1) (a_2 - a_1) in ulps
+            // when a_k's exponent is a_1's; otherwise the additions are done one by one.
+            const int k = min(max(g - o_prev, 0), 254);
             float a = s_al;
-            // the march's float32 alpha sequence: g - o_prev (< 255) additions from the run's first
-            for (int k = min(max(g - o_prev, 0), 254); k > 0; --k) a = __fadd_rn(a, step);
+            if (k > 0) {
+                const float a1 = __fadd_rn(s_al, step), a2 = __fadd_rn(a1, step);
+                const uint32_t b1 = __float_as_uint(a1);
+                const uint32_t cand = b1 + (uint32_t)(k - 1) * (__float_as_uint(a2) - b1);
+                if ((cand >> 23) == (b1 >> 23) && (b1 >> 23) != 0u && (b1 >> 31) == 0u) {
+                    a = __uint_as_float(cand);
+                } else {
+                    for (int j = k; j > 0; --j) a = __fadd_rn(a, step);
+                }
+            }
             mixed_sample<M>(P, sh, lane, a, s_owner, s_w, s_word);
         }
     }
@@ -435,7 +453,7 @@ __global__ void __launch_bounds__(kBlockThreads, M <= 4 ? 7 : 5) adjoint_kernel(
     // into their samples, which the warp evaluates 32 at a time.
     auto drain = [&](int first, int count) {
         const bool mine = lane < count;
-        const int e = (first + lane) & (kAdjQueue - 1);
+        const int e = (first + lane) & (kRunQueue - 1);
         float al = 0.0f, wrun = 1.0f;
         int kn = 0, owner = 0;
         uint32_t word = 0, w1 = 0;
@@ -476,46 +494,53 @@ __global__ void __launch_bounds__(kBlockThreads, M <= 4 ? 7 : 5) adjoint_kernel(
                     for (int c = 0; c < 8; c++)
                         r8[c] = tex3D<float>(P.density_point, bx + (float)(c & 1) + 0.5f,
                                              by + (float)((c >> 1) & 1) + 0.5f, bz + (float)(c >> 2) + 0.5f);
-                    // grad rho = c0 + c1 f_a + c2 f_b + c3 f_a f_b per axis (f_a, f_b the other two
-                    // fractions), summed over the run's samples f0 + k d, alpha0 + k delta in closed form
-                    const float ax = __fsub_rn(px, bx), ay = __fsub_rn(py, by), az = __fsub_rn(pz, bz);
-                    const float delta = __fsub_rn(__fadd_rn(al, step), al);  // the float32 step at alpha0
-                    const float bxs = delta * rxi, bys = delta * ryi, bzs = delta * rzi;
-                    const float ex = r8[1] - r8[0], ey = r8[2] - r8[0], ez = r8[4] - r8[0];
-                    const float x1 = (r8[3] - r8[2]) - ex, x2 = (r8[5] - r8[4]) - ex;
-                    const float x3 = (r8[7] - r8[6]) - (r8[5] - r8[4]) - (r8[3] - r8[2]) + ex;
-                    const float y1 = (r8[3] - r8[1]) - ey, y2 = (r8[6] - r8[4]) - ey;
-                    const float y3 = (r8[7] - r8[5]) - (r8[6] - r8[4]) - (r8[3] - r8[1]) + ey;
-                    const float z1 = (r8[5] - r8[1]) - ez, z2 = (r8[6] - r8[2]) - ez;
-                    const float z3 = (r8[7] - r8[3]) - (r8[6] - r8[2]) - (r8[5] - r8[1]) + ez;
-                    // about the run's middle sample k_c = (K - 1) / 2 the odd sums of k - k_c vanish:
-                    // sum g(f_k) and sum alpha_k g(f_k) need only S2 = sum (k - k_c)^2 = K (K^2 - 1) / 12
-                    const float kf = (float)kn;
-                    const float kc = 0.5f * kf - 0.5f;
-                    const float cx = ax + kc * bxs, cy = ay + kc * bys, cz = az + kc * bzs;
-                    const float ac = al + kc * delta;
-                    const float S2 = kf * (kf * kf - 1.0f) * (1.0f / 12.0f);
-                    const float dS2 = delta * S2;
-                    float h[3], hk[3];
-                    float m = kf, n = ac * kf;  // g = 1
-                    h[0] = ex * m, h[1] = ey * m, h[2] = ez * m;
-                    hk[0] = ex * n, hk[1] = ey * n, hk[2] = ez * n;
-                    m = kf * cx, n = ac * m + dS2 * bxs;  // g = f_x
-                    h[1] += y1 * m, h[2] += z1 * m, hk[1] += y1 * n, hk[2] += z1 * n;
-                    m = kf * cy, n = ac * m + dS2 * bys;  // g = f_y
-                    h[0] += x1 * m, h[2] += z2 * m, hk[0] += x1 * n, hk[2] += z2 * n;
-                    m = kf * cz, n = ac * m + dS2 * bzs;  // g = f_z
-                    h[0] += x2 * m, h[1] += y2 * m, hk[0] += x2 * n, hk[1] += y2 * n;
-                    m = kf * cx * cy + bxs * bys * S2, n = ac * m + dS2 * (cx * bys + cy * bxs);  // g = f_x f_y
-                    h[2] += z3 * m, hk[2] += z3 * n;
-                    m = kf * cx * cz + bxs * bzs * S2, n = ac * m + dS2 * (cx * bzs + cz * bxs);  // g = f_x f_z
-                    h[1] += y3 * m, hk[1] += y3 * n;
-                    m = kf * cy * cz + bys * bzs * S2, n = ac * m + dS2 * (cy * bzs + cz * bys);  // g = f_y f_z
-                    h[0] += x3 * m, hk[0] += x3 * n;
-                    const float gw = gu * wrun;
+                    // a cell whose eight texels are equal (and finite) has grad rho = 0: its pose
+                    // terms are exactly zero, and a warp whose runs all lie in such cells skips them
+                    bool flat = fabsf(r8[0]) < __int_as_float(0x7f800000);
 #pragma unroll
-                    for (int c = 0; c < 3; c++) h[c] *= gw, hk[c] *= gw;
-                    add_pose(h, hk, owner);
+                    for (int c = 1; c < 8; c++) flat = flat && r8[c] == r8[0];
+                    if (!flat) {
+                        // grad rho = c0 + c1 f_a + c2 f_b + c3 f_a f_b per axis (f_a, f_b the other two
+                        // fractions), summed over the run's samples f0 + k d, alpha0 + k delta in closed form
+                        const float ax = __fsub_rn(px, bx), ay = __fsub_rn(py, by), az = __fsub_rn(pz, bz);
+                        const float delta = __fsub_rn(__fadd_rn(al, step), al);  // the float32 step at alpha0
+                        const float bxs = delta * rxi, bys = delta * ryi, bzs = delta * rzi;
+                        const float ex = r8[1] - r8[0], ey = r8[2] - r8[0], ez = r8[4] - r8[0];
+                        const float x1 = (r8[3] - r8[2]) - ex, x2 = (r8[5] - r8[4]) - ex;
+                        const float x3 = (r8[7] - r8[6]) - (r8[5] - r8[4]) - (r8[3] - r8[2]) + ex;
+                        const float y1 = (r8[3] - r8[1]) - ey, y2 = (r8[6] - r8[4]) - ey;
+                        const float y3 = (r8[7] - r8[5]) - (r8[6] - r8[4]) - (r8[3] - r8[1]) + ey;
+                        const float z1 = (r8[5] - r8[1]) - ez, z2 = (r8[6] - r8[2]) - ez;
+                        const float z3 = (r8[7] - r8[3]) - (r8[6] - r8[2]) - (r8[5] - r8[1]) + ez;
+                        // about the run's middle sample k_c = (K - 1) / 2 the odd sums of k - k_c vanish:
+                        // sum g(f_k) and sum alpha_k g(f_k) need only S2 = sum (k - k_c)^2 = K (K^2 - 1) / 12
+                        const float kf = (float)kn;
+                        const float kc = 0.5f * kf - 0.5f;
+                        const float cx = ax + kc * bxs, cy = ay + kc * bys, cz = az + kc * bzs;
+                        const float ac = al + kc * delta;
+                        const float S2 = kf * (kf * kf - 1.0f) * (1.0f / 12.0f);
+                        const float dS2 = delta * S2;
+                        float h[3], hk[3];
+                        float m = kf, n = ac * kf;  // g = 1
+                        h[0] = ex * m, h[1] = ey * m, h[2] = ez * m;
+                        hk[0] = ex * n, hk[1] = ey * n, hk[2] = ez * n;
+                        m = kf * cx, n = ac * m + dS2 * bxs;  // g = f_x
+                        h[1] += y1 * m, h[2] += z1 * m, hk[1] += y1 * n, hk[2] += z1 * n;
+                        m = kf * cy, n = ac * m + dS2 * bys;  // g = f_y
+                        h[0] += x1 * m, h[2] += z2 * m, hk[0] += x1 * n, hk[2] += z2 * n;
+                        m = kf * cz, n = ac * m + dS2 * bzs;  // g = f_z
+                        h[0] += x2 * m, h[1] += y2 * m, hk[0] += x2 * n, hk[1] += y2 * n;
+                        m = kf * cx * cy + bxs * bys * S2, n = ac * m + dS2 * (cx * bys + cy * bxs);  // g = f_x f_y
+                        h[2] += z3 * m, hk[2] += z3 * n;
+                        m = kf * cx * cz + bxs * bzs * S2, n = ac * m + dS2 * (cx * bzs + cz * bxs);  // g = f_x f_z
+                        h[1] += y3 * m, hk[1] += y3 * n;
+                        m = kf * cy * cz + bys * bzs * S2, n = ac * m + dS2 * (cy * bzs + cz * bys);  // g = f_y f_z
+                        h[0] += x3 * m, hk[0] += x3 * n;
+                        const float gw = gu * wrun;
+    #pragma unroll
+                        for (int c = 0; c < 3; c++) h[c] *= gw, hk[c] *= gw;
+                        add_pose(h, hk, owner);
+                    }
                 }
             }
         }
@@ -556,18 +581,20 @@ __global__ void __launch_bounds__(kBlockThreads, M <= 4 ? 7 : 5) adjoint_kernel(
         const unsigned pm = __ballot_sync(kAll, push);
         {
             // a lane that closes no run stores into its own slot past the ring
-            const int s = push ? (head + queued + __popc(pm & lt)) & (kAdjQueue - 1) : kAdjQueue + lane;
+            const int s = push ? (head + queued + __popc(pm & lt)) & (kRunQueue - 1) : kRunQueue + lane;
             sh.runa[s] = make_uint4(__float_as_uint(a0), (uint32_t)K | ((uint32_t)lane << 8) | (half ? 1u << 13 : 0u),
                                     SX, S0);
             sh.runb[s] = make_uint2(S1, SZ);
             K = push ? 0 : K;
         }
         queued += __popc(pm);
-        if (queued >= 32) {
+    };
+    auto settle = [&]() {  // drain while 32 runs wait (warp-uniform); one call site per loop iteration
+        while (queued >= 32) {
             __syncwarp();
             drain(head, 32);
             __syncwarp();
-            head = (head + 32) & (kAdjQueue - 1);
+            head = (head + 32) & (kRunQueue - 1);
             queued -= 32;
         }
     };
@@ -587,6 +614,7 @@ __global__ void __launch_bounds__(kBlockThreads, M <= 4 ? 7 : 5) adjoint_kernel(
             K = 1;
         }
         enqueue(here, true);
+        settle();
     };
 
     single(first_half);
@@ -603,26 +631,32 @@ __global__ void __launch_bounds__(kBlockThreads, M <= 4 ? 7 : 5) adjoint_kernel(
     const int warp_steps = __reduce_max_sync(kAll, my_steps) + 1;
     float alpha_end = alpha;
     advance_alpha(&alpha_end, step, __int_as_float(0x7f800000), my_steps, false);
-    float cx = __fsub_rn(__fmaf_rn(alpha, R.rxi, R.sx), 1.0f);
-    float cy = __fsub_rn(__fmaf_rn(alpha, R.ryi, R.sy), 1.0f);
+    // x and y travel as f32x2 pairs (the same roundings as the scalar operations)
+    const float2 r2 = make_float2(R.rxi, R.ryi), s2 = make_float2(R.sx, R.sy);
+    const float2 one2 = make_float2(1.0f, 1.0f), half2v = make_float2(0.5f, 0.5f);
+    const float2 f256 = make_float2(256.0f, 256.0f), fofs = make_float2(-127.5f, -127.5f);
+    const float2 step2 = make_float2(step, step);
+    float2 a2 = make_float2(alpha, alpha);
+    float2 c2 = sub2_rn(fma2_rn(a2, r2, s2), one2);
     float cz = __fsub_rn(__fmaf_rn(alpha, R.rzi, R.sz), 1.0f);
-#pragma unroll 2
-    for (int it = 0; it < warp_steps; ++it) {
+    auto march_step = [&](int it) {
         const bool live = it < my_steps;
-        const float bx = floorf(cx), by = floorf(cy), bz = floorf(cz);
+        const float bx = floorf(c2.x), by = floorf(c2.y), bz = floorf(cz);
         int fxi = 0, fyi = 0, fzi = 0;
         // Each axis's position, label cell and fixed point are monotone in alpha (every operation
         // producing them is a monotone rounding), so a sample whose cells equal the previous
         // sample's has the cells of the whole open run: comparing with the previous sample suffices.
-        bool fresh = K == 0 || K == 255 || bx != rbx || by != rby || bz != rbz;
+        bool fresh = K == 255 || bx != rbx || by != rby || bz != rbz;
         if (do_dens) {
-            fxi = hw_fix_live(cx), fyi = hw_fix_live(cy), fzi = hw_fix_live(cz);
+            // hw_fix_live of x and y as one pair
+            const float2 q2 = fma2_rn(add2_rn(c2, half2v), f256, fofs);
+            fxi = (int)__float2uint_rd(q2.x), fyi = (int)__float2uint_rd(q2.y), fzi = hw_fix_live(cz);
             fresh = fresh || ((fxi ^ rfx) | (fyi ^ rfy) | (fzi ^ rfz)) >= 256;
         }
         // a run ends when this sample starts a new one or the ray has no full-weight samples left
         enqueue(K > 0 && (!live || fresh), false);
         const bool open = live && K == 0;  // this sample starts a run
-        a0 = open ? alpha : a0;
+        a0 = open ? a2.x : a0;
         if (do_dens) {
             uint32_t hx, hy0, hy1;
             const uint32_t Az = (uint32_t)fzi & 255u;
@@ -636,10 +670,17 @@ __global__ void __launch_bounds__(kBlockThreads, M <= 4 ? 7 : 5) adjoint_kernel(
         rbx = bx, rby = by, rbz = bz;
         rfx = fxi, rfy = fyi, rfz = fzi;
         K += live ? 1 : 0;
-        alpha = __fadd_rn(alpha, step);
-        cx = __fsub_rn(__fmaf_rn(alpha, R.rxi, R.sx), 1.0f);
-        cy = __fsub_rn(__fmaf_rn(alpha, R.ryi, R.sy), 1.0f);
-        cz = __fsub_rn(__fmaf_rn(alpha, R.rzi, R.sz), 1.0f);
+        a2 = add2_rn(a2, step2);
+        c2 = sub2_rn(fma2_rn(a2, r2, s2), one2);
+        cz = __fsub_rn(__fmaf_rn(a2.x, R.rzi, R.sz), 1.0f);
+    };
+    // two steps per iteration and one drain site: at most 64 runs are pushed before the ring is
+    // settled, so it holds 128. A step past warp_steps closes and opens nothing (every lane has
+    // closed its last run by then).
+    for (int it = 0; it < warp_steps; it += 2) {
+        march_step(it);
+        march_step(it + 1);
+        settle();
     }
     alpha = alpha_end;
     single(last_half);
