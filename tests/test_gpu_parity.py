@@ -30,9 +30,9 @@ pytestmark = pytest.mark.gpu
 
 
 def run_product(volumes, projs, *, spectrum="90KV_AL40", source=None, priorities=None, attenuate=False,
-                flags=0, density_dtype="float32", solid_angle=False):
+                flags=0, density_dtype="float32", solid_angle=False, step=0.1):
     src = source or tables.NpzTables(GOLDEN_TABLES)
-    p = dd.Projector(volumes, priorities=priorities, spectrum=spectrum, step=0.1, tables=src, neglog=False,
+    p = dd.Projector(volumes, priorities=priorities, spectrum=spectrum, step=step, tables=src, neglog=False,
                      attenuate_outside_volume=attenuate, density_dtype=density_dtype)
     with p:
         out = p.project_tensors(*projs, area_density=True, solid_angle=solid_angle, flags=flags)
@@ -147,6 +147,31 @@ def test_multi_volume_matches_oracle_and_full_march():
         assert rel_err(got["intensity"][i], ref["intensity"]).max() <= 2e-6
         d = np.abs(got["area_density"][i] - ref["area_density"])
         assert np.all(d <= 2e-6 * np.abs(ref["area_density"]) + 1e-7), d.max()
+
+
+@pytest.mark.parametrize("step", [0.55, 1.7])
+def test_long_steps_match_oracle_and_full_march(step):
+    """A march reads its label codes without clamps only where its first base and its look-ahead
+    base (one step past its last sample) lie in the code table ([-2, n-1] per axis); a step longer
+    than half a voxel carries the look-ahead of rays leaving through a low face past it, so those
+    rays (and multi-volume stretches) read through the clamps. Both kinds against the float32 oracle
+    (2e-6) and against the reference's full march, which always clamps, bit for bit."""
+    rng = np.random.default_rng(9)
+    a = volume_from_hu(simple_phantom_hu(32, seed=9))
+    b = volume_from_hu(simple_phantom_hu(20, seed=10), spacing=(1.3, 1.3, 1.3))
+    b.world_from_anatomical = random_rigid(rng, 6.0, 20.0)
+    projs = random_views(2, a.center_in_world, seed=12, sphere_mm=5.0, cone_deg=60.0, sensor_size=(20, 18),
+                         pixel_size=3.0)
+    for vols in ([a], [a, b]):
+        got = run_product(vols, projs, step=step)
+        full = run_product(vols, projs, step=step, flags=_lib.DRR_FLAG_FULL_MARCH)
+        for k in ("intensity", "area_density"):
+            np.testing.assert_array_equal(got[k], full[k])
+        for i, proj in enumerate(projs):
+            ref = oracle_scene(vols, proj, step=step).project("f32")
+            assert rel_err(got["intensity"][i], ref["intensity"]).max() <= 2e-6
+            d = np.abs(got["area_density"][i] - ref["area_density"])
+            assert np.all(d <= 2e-6 * np.abs(ref["area_density"]) + 1e-7), d.max()
 
 
 @pytest.mark.parametrize("nvol", [3, 4])
