@@ -32,14 +32,17 @@ def _rotation(rng, deg):
     return np.eye(3) + np.sin(th) * K + (1 - np.cos(th)) * K @ K
 
 
-def test_range_holds_every_coincidence(shim):
-    rng = np.random.default_rng(0)
+@pytest.mark.parametrize("trials, reach, alpha_max, seed", [(400, 300.0, 2.0, 0), (1500, 2000.0, 3000.0, 123)])
+def test_range_holds_every_coincidence(shim, trials, reach, alpha_max, seed):
+    """Sources up to `reach` voxels from the grids' origins and marches starting at alpha up to
+    `alpha_max` (then 6000 steps): the float32 range's rounding grows with |s| and |alpha r|."""
+    rng = np.random.default_rng(seed)
     total_seen = 0
-    for trial in range(400):
+    for trial in range(trials):
         nv = int(rng.integers(2, 5))
         ray = rng.normal(size=3)
         ray /= np.linalg.norm(ray)
-        src = rng.uniform(-300, 300, 3)
+        src = rng.uniform(-reach, reach, 3)
         s, r = [], []
         base_A = np.diag(1.0 / rng.uniform(0.5, 1.5, 3)) @ _rotation(rng, rng.uniform(0, 180))
         base_o = rng.uniform(0, 100, 3)
@@ -61,7 +64,7 @@ def test_range_holds_every_coincidence(shim):
         r = np.ascontiguousarray(np.array(r, dtype=np.float32))
         step = float(rng.choice([0.1, 0.25, 0.05, 1.0]))
         seen = ctypes.c_int(0)
-        outside = shim.check_range(nv, s.ctypes.data, r.ctypes.data, step, float(rng.uniform(0.5, 2.0)), 6000,
+        outside = shim.check_range(nv, s.ctypes.data, r.ctypes.data, step, float(rng.uniform(0.5, alpha_max)), 6000,
                                    ctypes.byref(seen))
         total_seen += seen.value
         assert outside == 0, (trial, nv, step, seen.value)
