@@ -398,10 +398,12 @@ __device__ __forceinline__ void drain_mixed(const AdjointParams &P, AdjointWarpS
 // each warp 8 x 4 pixels). A run is a stretch of a ray's full-weight samples with one label cell
 // and one texture-filter cell; the trapezoid half-weight samples (t = 0 and t = num_steps - 1) are
 // runs of their own. See the file comment. Resident blocks per SM balance occupancy against the
-// registers the drain needs: with 3 materials, 7 blocks (72 registers, no spills) measured 0.888
-// ms/view against 0.906 at 6 blocks on the 256^3 / 64 x 256^2 workload. More materials keep 5.
+// registers the drain needs: with 3 materials and the drain's texel fetches issued before its
+// label-code load, 6 blocks (80 registers, no spills) measured 0.780 ms/view on the 256^3 / 64 x
+// 256^2 workload, against 0.912 at 7 blocks (72 registers, spilling) and 0.813 at 7 blocks with the
+// fetches after the code. More materials keep 5.
 template <int M>
-__global__ void __launch_bounds__(kBlockThreads, M <= 4 ? 7 : 5) adjoint_kernel(const __grid_constant__ AdjointParams P) {
+__global__ void __launch_bounds__(kBlockThreads, M <= 4 ? 6 : 5) adjoint_kernel(const __grid_constant__ AdjointParams P) {
     __shared__ AdjointWarpSmem<M> smem[kBlockThreads / 32];
     const SceneParams<1> &p = P.s;
     const int lane = threadIdx.x & 31;
@@ -470,6 +472,15 @@ __global__ void __launch_bounds__(kBlockThreads, M <= 4 ? 7 : 5) adjoint_kernel(
             const float py = __fsub_rn(__fmaf_rn(al, ryi, sh.ray[4][owner]), 1.0f);
             const float pz = __fsub_rn(__fmaf_rn(al, rzi, sh.ray[5][owner]), 1.0f);
             const float bx = floorf(px), by = floorf(py), bz = floorf(pz);
+            // the cell's eight texels (pose), fetched before the label code so that both loads are
+            // in flight together
+            float r8[8];
+            if (do_pose) {
+#pragma unroll
+                for (int c = 0; c < 8; c++)
+                    r8[c] = tex3D<float>(P.density_point, bx + (float)(c & 1) + 0.5f,
+                                         by + (float)((c >> 1) & 1) + 0.5f, bz + (float)(c >> 2) + 0.5f);
+            }
             // the cell's label code; the packed word only for a run in a mixed cell
             const float cbx = fminf(fmaxf(bx, -1.0f), V.nm1[0]), cby = fminf(fmaxf(by, -1.0f), V.nm1[1]);
             const float cbz = fminf(fmaxf(bz, -1.0f), V.nm1[2]);
@@ -489,11 +500,6 @@ __global__ void __launch_bounds__(kBlockThreads, M <= 4 ? 7 : 5) adjoint_kernel(
                                  vals);
                 }
                 if (do_pose) {
-                    float r8[8];
-#pragma unroll
-                    for (int c = 0; c < 8; c++)
-                        r8[c] = tex3D<float>(P.density_point, bx + (float)(c & 1) + 0.5f,
-                                             by + (float)((c >> 1) & 1) + 0.5f, bz + (float)(c >> 2) + 0.5f);
                     // a cell whose eight texels are equal (and finite) has grad rho = 0: its pose
                     // terms are exactly zero, and a warp whose runs all lie in such cells skips them
                     bool flat = fabsf(r8[0]) < __int_as_float(0x7f800000);
