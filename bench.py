@@ -182,7 +182,7 @@ FORWARD_SOURCES = ("drr_forward.cuh", "drr_launch.cuh", "drr_alpha.h", "drr_coin
 
 def source_sha() -> str:
     """Hash of the forward kernel's sources (the files its instantiation units compile from), to tell
-    whether a saved ncu figure of that kernel still describes this build."""
+    whether a saved ncu figure of that kernel still describes the current sources."""
     h = hashlib.sha256()
     for p in sorted(ROOT / "deepdrr_gb300" / "csrc" / name for name in FORWARD_SOURCES):
         h.update(p.name.encode())

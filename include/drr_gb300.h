@@ -44,7 +44,7 @@ extern "C" {
 typedef enum {
     DRR_OK = 0,
     DRR_ERR_INVALID_ARGUMENT = 1, /* the reference raises ValueError / AssertionError here */
-    DRR_ERR_UNSUPPORTED = 2,      /* a size or mode this build does not implement */
+    DRR_ERR_UNSUPPORTED = 2,      /* a size or mode the library does not implement */
     DRR_ERR_CUDA = 3,             /* a CUDA runtime call failed; see drr_last_error() */
     DRR_ERR_OUT_OF_MEMORY = 4
 } drr_status;
