@@ -14,6 +14,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <vector>
 
 #include "../../include/drr_gb300.h"
 #include "drr_forward.cuh"
@@ -97,23 +98,53 @@ void free_volume(Volume &v) {
     if (v.density_point) cudaDestroyTextureObject(v.density_point);
     if (v.density_array) cudaFreeArray(v.density_array);
     if (v.coded) cudaFree(v.coded);
-    if (v.labels_tex) cudaDestroyTextureObject(v.labels_tex);
-    if (v.labels_array) cudaFreeArray(v.labels_array);
+    if (v.gen_words) cudaFree(v.gen_words);
+    if (v.gen_start) cudaFree(v.gen_start);
     v = Volume();
 }
 
-// Label codes of every base of a volume (see drr::pack_labels_kernel) and the labels as a uint8
-// texture, owned by the volume set: 2 bytes per base plus 1 byte per voxel.
+// Label codes of every base of a volume (see drr::pack_labels_kernel), owned by the volume set: 2
+// bytes per base. The neighbourhoods of three or more labels (rare in CT) get their packed labels
+// in a side table, numbered within segments of kGeneralSegment bases of a code-table row so that a
+// number fits the codes' 11 free bits (drr::index_general_kernel): 4 bytes each, plus 4 bytes per
+// segment for its first index.
 drr_status make_label_tables(const uint8_t *src, int ni, int nj, int nk, cudaStream_t s, Volume &v) {
-    const size_t np = (size_t)(ni + 2) * (nj + 2) * (nk + 2);
+    const size_t row = (size_t)ni + 2, plane = row * (nj + 2), np = plane * (nk + 2);
     DRR_CUDA_TRY(cudaMalloc(&v.coded, np * sizeof(uint16_t)), "cudaMalloc (label codes)");
-    const drr_status st = make_texture(src, 1, cudaCreateChannelDesc(8, 0, 0, 0, cudaChannelFormatKindUnsigned),
-                                       false, ni, nj, nk, s, &v.labels_array, &v.labels_tex);
-    if (st != DRR_OK) return st;
     const size_t blocks = (np + 255) / 256;
     drr::pack_labels_kernel<<<(unsigned)(blocks < 1048576 ? blocks : 1048576), 256, 0, s>>>(src, ni, nj, nk,
                                                                                            v.coded);
     DRR_CUDA_TRY(cudaGetLastError(), "pack_labels_kernel launch");
+    const size_t segs = (size_t)(nk + 2) * (nj + 2) * drr::general_segments_per_row(ni);
+    const unsigned seg_blocks = (unsigned)((segs + 7) / 8 < 1048576 ? (segs + 7) / 8 : 1048576);  // 8 warps each
+    DRR_CUDA_TRY(cudaMalloc(&v.gen_start, sizeof(uint32_t) * (segs + 1)), "cudaMalloc (general index)");
+    drr::count_general_kernel<<<seg_blocks, 256, 0, s>>>(v.coded, ni, nj, nk, v.gen_start);
+    DRR_CUDA_TRY(cudaGetLastError(), "count_general_kernel launch");
+    std::vector<uint32_t> start(segs + 1);
+    DRR_CUDA_TRY(cudaMemcpyAsync(start.data(), v.gen_start, sizeof(uint32_t) * segs, cudaMemcpyDeviceToHost, s),
+                 "general counts download");
+    DRR_CUDA_TRY(cudaStreamSynchronize(s), "general counts download");
+    uint64_t total = 0;  // counts to first indices (exclusive sums)
+    for (size_t g = 0; g < segs; g++) {
+        const uint64_t c = start[g];
+        start[g] = (uint32_t)total;
+        total += c;
+    }
+    if (total > 0xFFFFFFFFull) return drr::fail(DRR_ERR_UNSUPPORTED, "drr_volset_create: too many neighbourhoods of three or more labels");
+    start[segs] = (uint32_t)total;
+    DRR_CUDA_TRY(cudaMalloc(&v.gen_words, sizeof(uint32_t) * (total > 0 ? total : 1)), "cudaMalloc (general words)");
+    DRR_CUDA_TRY(cudaMemcpyAsync(v.gen_start, start.data(), sizeof(uint32_t) * (segs + 1), cudaMemcpyHostToDevice, s),
+                 "general index upload");
+    drr::index_general_kernel<<<seg_blocks, 256, 0, s>>>(src, ni, nj, nk, v.coded, v.gen_start, v.gen_words);
+    DRR_CUDA_TRY(cudaGetLastError(), "index_general_kernel launch");
+    // rows of bases j = -2 and the plane of bases k = -2 hold the same neighbourhoods as those of -1:
+    // copy their codes, numbers included, so that a lookup may clamp j and k to -1
+    DRR_CUDA_TRY(cudaMemcpy2DAsync(v.coded, plane * sizeof(uint16_t), v.coded + row, plane * sizeof(uint16_t),
+                                   row * sizeof(uint16_t), (size_t)nk + 2, cudaMemcpyDeviceToDevice, s),
+                 "label codes of the base rows -2");
+    DRR_CUDA_TRY(cudaMemcpyAsync(v.coded, v.coded + plane, plane * sizeof(uint16_t), cudaMemcpyDeviceToDevice, s),
+                 "label codes of the base plane -2");
+    DRR_CUDA_TRY(cudaStreamSynchronize(s), "general index upload");  // `start` is a host vector
     return DRR_OK;
 }
 
@@ -151,6 +182,66 @@ __global__ void pack_labels_kernel(const uint8_t *__restrict__ labels, int ni, i
                 general = true;
         }
         coded[e] = (uint16_t)(general ? (kCodeGeneral | A) : (A | (B << 4) | (mask << 8)));
+    }
+}
+
+// Neighbourhoods of three or more labels in each segment of kGeneralSegment bases of a code-table
+// row, one warp per segment (segment g: row g / segs_per_row, bases (g % segs_per_row) * kGeneralSegment
+// onwards).
+__global__ void count_general_kernel(const uint16_t *__restrict__ coded, int ni, int nj, int nk, uint32_t *counts) {
+    const size_t row = (size_t)ni + 2;
+    const size_t spr = general_segments_per_row(ni);
+    const size_t segs = (size_t)(nk + 2) * (nj + 2) * spr;
+    const int lane = threadIdx.x & 31;
+    for (size_t g = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < segs;
+         g += ((size_t)gridDim.x * blockDim.x) >> 5) {
+        const size_t r = g / spr, i0 = (g % spr) * kGeneralSegment;
+        const size_t i1 = i0 + kGeneralSegment < row ? i0 + kGeneralSegment : row;
+        uint32_t c = 0;
+        for (size_t i = i0 + lane; i < i1; i += 32) c += (coded[r * row + i] & kCodeGeneral) ? 1u : 0u;
+        for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+        if (lane == 0) counts[g] = c;
+    }
+}
+
+// Numbers the neighbourhoods of three or more labels of each row segment in table order (one warp
+// per segment), stores each one's packed labels (4 bits per corner: the eight labels the reference
+// fetches, at clamp(b + d, 0, n - 1)) at words[start[g] + number] and the number (below
+// kGeneralSegment) in its code's free bits: 4-7 the low four, 9-15 the high seven.
+__global__ void index_general_kernel(const uint8_t *__restrict__ labels, int ni, int nj, int nk, uint16_t *coded,
+                                     const uint32_t *__restrict__ start, uint32_t *words) {
+    const size_t row = (size_t)ni + 2;
+    const size_t spr = general_segments_per_row(ni);
+    const size_t segs = (size_t)(nk + 2) * (nj + 2) * spr;
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    for (size_t g = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < segs;
+         g += ((size_t)gridDim.x * blockDim.x) >> 5) {
+        const size_t r = g / spr, i0 = (g % spr) * kGeneralSegment;
+        const size_t i1 = i0 + kGeneralSegment < row ? i0 + kGeneralSegment : row;
+        const int bj = (int)(r % (size_t)(nj + 2)) - 2, bk = (int)(r / (size_t)(nj + 2)) - 2;
+        uint32_t running = 0;
+        for (size_t ib = i0; ib < i1; ib += 32) {
+            const size_t i = ib + lane;
+            uint16_t *pc = coded + r * row + i;
+            const bool gen = i < i1 && (*pc & kCodeGeneral);
+            const unsigned b = __ballot_sync(0xffffffffu, gen);
+            if (gen) {
+                const uint32_t number = running + __popc(b & lt);
+                const int bi = (int)i - 2;
+                uint32_t word = 0;
+#pragma unroll
+                for (int c = 0; c < 8; c++) {
+                    const int ii = clampi(bi + (c & 1), 0, ni - 1);
+                    const int jj = clampi(bj + ((c >> 1) & 1), 0, nj - 1);
+                    const int kk = clampi(bk + (c >> 2), 0, nk - 1);
+                    word |= ((uint32_t)labels[((size_t)kk * nj + jj) * ni + ii] & 15u) << (4 * c);
+                }
+                words[start[g] + number] = word;
+                *pc = (uint16_t)((*pc & (kCodeGeneral | 15u)) | ((number & 15u) << 4) | ((number >> 4) << 9));
+            }
+            running += __popc(b);
+        }
     }
 }
 }  // namespace drr

@@ -63,8 +63,8 @@ struct VolConst {
     cudaTextureObject_t density;  // linear filter, clamp, unnormalised coordinates
     const uint16_t *coded;        // label codes [(nk+2)][(nj+2)][(ni+2)] (pack_labels_kernel), at the entry of
                                   // base (0, 0, 0): bases run from -2 to n - 1 on each axis
-    cudaTextureObject_t labels;   // the labels themselves (uint8, point filter, clamp), read for neighbourhoods
-                                  // of three or more labels
+    const uint32_t *gen_words;    // packed labels of the neighbourhoods of three or more labels, numbered
+    const uint32_t *gen_start;    // per row segment of the code table (general_label_word)
     int32_t n[3];                 // ni, nj, nk
     float hi[3];                  // n - 0.5 per axis (projector.py:1626-1634)
     float nm1[3];                 // n - 1 per axis
@@ -261,39 +261,42 @@ __device__ __forceinline__ bool direct_bases(const VolConst &V, float2 b0xy, flo
            b0z >= -2.0f && b1z >= -2.0f && b0z <= V.nm1[2] && b1z <= V.nm1[2];
 }
 
+// Neighbourhoods of three or more labels are numbered within segments of kGeneralSegment bases of
+// a code-table row, so that a number fits the 11 bits a code of such a neighbourhood leaves free.
+constexpr int kGeneralSegment = 2048;
+__host__ __device__ __forceinline__ unsigned general_segments_per_row(int ni) {
+    return (unsigned)(ni + 2 + kGeneralSegment - 1) / (unsigned)kGeneralSegment;
+}
+
 // The packed word of a neighbourhood of three or more labels, 4 bits per corner (corner c at bits
-// 4c..4c+3): the eight texels the reference fetches, read from a uint8 label texture with point
-// filtering and clamp addressing (as projector.py:1500-1519 creates the reference's), at b + d + 0.5,
-// whose texel is clamp(b + d, 0, n - 1). Such neighbourhoods are rare (well under 1 % of a CT's
-// cells): the loop stays rolled so that it needs few registers besides the march's own.
-__device__ __forceinline__ uint32_t gather_label_word(cudaTextureObject_t labels, float bx, float by, float bz) {
-    uint32_t word = 0;
-#pragma unroll 1
-    for (int c = 0; c < 8; c++) {
-        const float x = bx + (float)(c & 1) + 0.5f, y = by + (float)((c >> 1) & 1) + 0.5f, z = bz + (float)(c >> 2) + 0.5f;
-        word |= ((uint32_t)tex3D<unsigned char>(labels, x, y, z) & 15u) << (4 * c);
-    }
-    return word;
+// 4c..4c+3: the eight texels the reference fetches with point filtering and clamp addressing,
+// projector.py:1500-1519, at b + d + 0.5, whose texel is clamp(b + d, 0, n - 1)), whose code `code`
+// was read at base (bx, by, bz), clamped to the table or not. The code carries the neighbourhood's
+// number in its row segment (bits 4-7 and 9-15; drr_volset_create numbers them), so the word is
+// two loads: the segment's first index and the word. The table's rows and plane of bases -2 are
+// copies of those of -1, numbers included, so j and k are clamped to [-1, n - 1] here, and i only
+// chooses the segment, which bases -2 and -1 share.
+__device__ __forceinline__ uint32_t general_label_word(const VolConst &V, uint32_t code, float bx, float by, float bz) {
+    const int i = (int)fminf(fmaxf(bx, -1.0f), V.nm1[0]);
+    const int j = (int)fminf(fmaxf(by, -1.0f), V.nm1[1]);
+    const int k = (int)fminf(fmaxf(bz, -1.0f), V.nm1[2]);
+    const unsigned seg = ((unsigned)(k + 2) * (unsigned)(V.n[1] + 2) + (unsigned)(j + 2)) * general_segments_per_row(V.n[0]) +
+                         (unsigned)(i + 2) / (unsigned)kGeneralSegment;
+    const uint32_t number = ((code >> 4) & 15u) | ((code >> 9) << 4);
+    return __ldg(V.gen_words + __ldg(V.gen_start + seg) + number);
 }
 
 // The packed word of a neighbourhood from its code, 4 bits per corner; (bx, by, bz) is the base the
 // code belongs to. Codes of one or two labels expand arithmetically: the mask's bit c moves to bit
-// 4c, and the corners it marks take B instead of A; three or more labels are gathered.
+// 4c, and the corners it marks take B instead of A; three or more labels come from general_label_word.
 __device__ __forceinline__ uint32_t code_word(const VolConst &V, uint32_t code, float bx, float by, float bz) {
-    if (code & kCodeGeneral) return gather_label_word(V.labels, bx, by, bz);
+    if (code & kCodeGeneral) return general_label_word(V, code, bx, by, bz);
     const uint32_t A = code & 15u, B = (code >> 4) & 15u;
     uint32_t m = code >> 8;                    // bit c: corner c holds B
     m = (m | (m << 12)) & 0x000F000Fu;         // spread bit c to bit 4c
     m = (m | (m << 6)) & 0x03030303u;
     m = (m | (m << 3)) & 0x11111111u;
     return (A * 0x11111111u) ^ ((A ^ B) * m);
-}
-
-// The word of base b where its code is known to be kCodeGeneral (b clamped to [-1, n - 1] first,
-// which leaves every corner's clamped texel unchanged).
-__device__ __forceinline__ uint32_t general_label_word(const VolConst &V, float bx, float by, float bz) {
-    return gather_label_word(V.labels, fminf(fmaxf(bx, -1.0f), V.nm1[0]), fminf(fmaxf(by, -1.0f), V.nm1[1]),
-                             fminf(fmaxf(bz, -1.0f), V.nm1[2]));
 }
 
 __device__ __forceinline__ uint32_t fetch_label_word(const VolConst &V, float bx, float by, float bz) {
@@ -636,7 +639,7 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
                     for (int m = 0; m < M; m++)
                         ad[m] = __fmaf_rn(wr, (uint32_t)m == A ? sA : ((uint32_t)m == B ? sB : 0.0f), ad[m]);
                 } else {
-                    word = general_label_word(V, cb2.x, cb2.y, cbz);  // three or more labels: the corners' own
+                    word = general_label_word(V, code, cb2.x, cb2.y, cbz);  // three or more labels: the corners' own
                     float seg[M];
                     label_fractions<M>(word, cw, seg);
 #pragma unroll
@@ -836,11 +839,11 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
                     } else {
                         uint32_t w = 0u;
                         if (own) {
-                            w = general_label_word(p.vol[vol], bx, by, bz);
+                            w = general_label_word(p.vol[vol], code, bx, by, bz);
                         } else {
 #pragma unroll
                             for (int i = 0; i < NV; i++)
-                                if (i == key_vol) w = general_label_word(p.vol[i], pb0, pb1, pb2);
+                                if (i == key_vol) w = general_label_word(p.vol[i], code, pb0, pb1, pb2);
                         }
                         float seg[M];
                         label_fractions<M>(w, cw, seg);
@@ -948,7 +951,7 @@ __device__ __forceinline__ void render_ray(const SceneParams<NV> &p, const ViewR
                             ad[m] = __fmaf_rn(wr, (uint32_t)m == A ? sA : ((uint32_t)m == B ? sB : 0.0f), ad[m]);
                     } else {
                         float seg[M];
-                        label_fractions<M>(general_label_word(Vv, cb2.x, cb2.y, cbz), cw, seg);
+                        label_fractions<M>(general_label_word(Vv, c_cur, cb2.x, cb2.y, cbz), cw, seg);
 #pragma unroll
                         for (int m = 0; m < M; m++) ad[m] = __fmaf_rn(wr, seg[m], ad[m]);
                     }
@@ -1170,6 +1173,9 @@ __global__ void __launch_bounds__(kBlockThreads, forward_min_blocks<NV, M>()) fo
 // Codes the labels of every 2x2x2 neighbourhood: the code of base b in [-2, n-1]^3 describes the labels
 // at clamp(b + d, 0, n - 1), corner c = dx | dy << 1 | dz << 2 (the layout above kCodeGeneral).
 __global__ void pack_labels_kernel(const uint8_t *__restrict__ labels, int ni, int nj, int nk, uint16_t *coded);
+__global__ void count_general_kernel(const uint16_t *__restrict__ coded, int ni, int nj, int nk, uint32_t *counts);
+__global__ void index_general_kernel(const uint8_t *__restrict__ labels, int ni, int nj, int nk, uint16_t *coded,
+                                     const uint32_t *__restrict__ start, uint32_t *words);
 
 // Host-side launcher, explicitly instantiated per (NV, M) in drr_inst_nv*.cu.
 template <int NV, int M>

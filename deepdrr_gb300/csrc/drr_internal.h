@@ -17,10 +17,10 @@ struct Volume {
     cudaArray_t density_array = nullptr;
     cudaTextureObject_t density_tex = 0;
     cudaTextureObject_t density_point = 0;  // point-filtered view of density_array (made by the adjoint)
-    uint16_t *coded = nullptr;   // [(nk+1)][(nj+1)][(ni+1)] codes of the 2x2x2 label neighbourhoods
+    uint16_t *coded = nullptr;   // [(nk+2)][(nj+2)][(ni+2)] codes of the 2x2x2 label neighbourhoods
                                  // (A, B, corners labelled B; see pack_labels_kernel)
-    cudaArray_t labels_array = nullptr;     // the labels (uint8, extent (ni, nj, nk)) for neighbourhoods of
-    cudaTextureObject_t labels_tex = 0;     // three or more labels: point filter, clamp addressing
+    uint32_t *gen_words = nullptr;  // packed labels of the neighbourhoods of three or more labels, numbered
+    uint32_t *gen_start = nullptr;  // per segment of a code-table row (first index of each segment)
     int ni = 0, nj = 0, nk = 0;
     int density_type = DRR_DENSITY_F32;
 };

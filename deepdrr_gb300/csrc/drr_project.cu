@@ -67,7 +67,8 @@ void fill_scene(drr::SceneParams<NV> &p, const drr_volset *set, const drr_tables
         // code table addressed from the entry of base (0, 0, 0): two planes, two rows and two entries in
         const size_t origin = 2 * ((size_t)(v.ni + 2) * (size_t)(v.nj + 2) + (size_t)(v.ni + 2) + 1);
         p.vol[i].coded = v.coded ? v.coded + origin : nullptr;
-        p.vol[i].labels = v.labels_tex;
+        p.vol[i].gen_words = v.gen_words;
+        p.vol[i].gen_start = v.gen_start;
         p.vol[i].n[0] = v.ni;
         p.vol[i].n[1] = v.nj;
         p.vol[i].n[2] = v.nk;

@@ -246,6 +246,38 @@ def test_three_label_neighbourhoods_match_oracle_and_reference_kernel(nvol):
             assert rel_err(got["intensity"][i], rk["intensity"]).max() <= 1e-4
 
 
+@pytest.mark.parametrize("shape", [(30, 30, 8), (2100, 3, 3)])
+def test_three_label_words_from_the_side_table(shape):
+    """Neighbourhoods of three or more labels read their packed labels from a side table numbered
+    within segments of 2048 bases of a code-table row (the codes' 11 free bits). Random labels make
+    almost every neighbourhood such a one: a 30 x 30 x 8 volume (one segment per row) and a
+    2100 x 3 x 3 bar seen around its 2046th voxel, where its rows pass from the first segment to
+    the second. Bit-identical to the full march and within float32 rounding of the oracle, for one
+    volume and with a second one."""
+    rng = np.random.default_rng(shape[0])
+    names = ["air", "bone", "soft tissue", "titanium"]
+    dens = rng.uniform(0.1, 2.0, shape).astype(np.float32)
+    labs = rng.integers(0, 4, shape)
+    vol = dd.Volume.from_parameters(dens, {nm: labs == i for i, nm in enumerate(names)},
+                                    origin=-(np.asarray(shape) - 1) / 2.0, spacing=(1.0, 1.0, 1.0))
+    ijk = np.array([2046.0 if shape[0] > 2048 else (shape[0] - 1) / 2.0, (shape[1] - 1) / 2.0, (shape[2] - 1) / 2.0, 1.0])
+    center = (np.linalg.inv(np.asarray(vol.ijk_from_world.data, dtype=np.float64)) @ ijk)[:3]
+    other = volume_from_hu(simple_phantom_hu(20, seed=3), spacing=(1.2, 1.2, 1.2))
+    other.world_from_anatomical = random_rigid(rng, 4.0, 25.0)
+    projs = random_views(2, center, seed=44, sphere_mm=2.0, cone_deg=40.0, sensor_size=(20, 18), pixel_size=3.0)
+    for vols in ([vol], [vol, other]):
+        got = run_product(vols, projs)
+        full = run_product(vols, projs, flags=_lib.DRR_FLAG_FULL_MARCH)
+        for k in ("intensity", "area_density"):
+            np.testing.assert_array_equal(got[k], full[k])
+        assert np.count_nonzero(got["area_density"][:, 1:].sum(1)) > 0  # the rays cross the labelled volume
+        for i, proj in enumerate(projs):
+            ref = oracle_scene(vols, proj).project("f32")
+            assert rel_err(got["intensity"][i], ref["intensity"]).max() <= 2e-6
+            d = np.abs(got["area_density"][i] - ref["area_density"])
+            assert np.all(d <= 2e-6 * np.abs(ref["area_density"]) + 1e-7), d.max()
+
+
 def test_attenuate_outside_matches_oracle():
     vols, projs = small_scene(6)
     got = run_product(vols, projs, attenuate=True)
