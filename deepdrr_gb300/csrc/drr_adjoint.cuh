@@ -62,20 +62,6 @@ struct AdjointParams {
     float center[3];                    // rotation centre, world
 };
 
-// Trilinear gradient of eight corner values c = dx | dy << 1 | dz << 2 at fractions (fx, fy, fz).
-__device__ __forceinline__ void trilinear_grad(const float v[8], float fx, float fy, float fz, float gx, float gy,
-                                               float gz, float d[3]) {
-    d[0] = gz * (gy * (v[1] - v[0]) + fy * (v[3] - v[2])) + fz * (gy * (v[5] - v[4]) + fy * (v[7] - v[6]));
-    d[1] = gz * (gx * (v[2] - v[0]) + fx * (v[3] - v[1])) + fz * (gx * (v[6] - v[4]) + fx * (v[7] - v[5]));
-    d[2] = gy * (gx * (v[4] - v[0]) + fx * (v[5] - v[1])) + fy * (gx * (v[6] - v[2]) + fx * (v[7] - v[3]));
-}
-
-__device__ __forceinline__ float trilinear(const float v[8], float fx, float fy, float fz, float gx, float gy,
-                                           float gz) {
-    return gz * (gy * (gx * v[0] + fx * v[1]) + fy * (gx * v[2] + fx * v[3])) +
-           fz * (gy * (gx * v[4] + fx * v[5]) + fy * (gx * v[6] + fx * v[7]));
-}
-
 // Per-ray state of the adjoint: the upstream material weights and the forward's march.
 template <int M>
 struct AdjointRay {
