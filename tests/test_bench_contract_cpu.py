@@ -28,3 +28,24 @@ def test_reference_arm_prints_one_contract_line():
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == line["value"]
     e2e = line["e2e"]
     assert e2e["value"] == line["value"] and e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
+
+
+def test_profile_figures_are_tied_to_the_forward_kernel_sources():
+    """bench.py marks the ncu figures it reports as stale when the forward kernel's sources change:
+    the files it hashes exist and are the ones the forward kernel's instantiation units include,
+    and the committed figures carry a hash of that form."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    csrc = ROOT / "deepdrr_gb300" / "csrc"
+    for name in bench.FORWARD_SOURCES:
+        assert (csrc / name).exists(), name
+    # the instantiation units include the launch header, which includes the forward kernel's
+    launch = (csrc / "drr_launch.cuh").read_text()
+    assert '#include "drr_forward.cuh"' in launch
+    forward = (csrc / "drr_forward.cuh").read_text()
+    for inc in ("drr_alpha.h", "drr_coincide.h"):
+        assert f'#include "{inc}"' in forward and inc in bench.FORWARD_SOURCES
+    figures = bench.read_profile_figures()
+    assert len(figures["source_sha"]) == len(bench.source_sha()) == 16
+    assert 0 < figures["tex_pipe_pct"] <= 100 and figures["dram_bytes_per_launch"] > 0
